@@ -1,0 +1,184 @@
+/*
+ * vesper_gb300.h -- C ABI of the GB300 (sm_103a) VESPER alignment hot path.
+ *
+ * Plain pointers and sizes only.  Unless stated otherwise every array
+ * argument is DEVICE memory owned by the caller, laid out C-order with the
+ * reference's [x][y][z] voxel indexing (VESPER_1_prob_new.py:43), and every
+ * call is asynchronous on ``stream`` (a cudaStream_t passed as void*; NULL
+ * means the legacy default stream).  No entry point allocates device memory:
+ * scratch space is a caller-provided ``workspace`` whose size the matching
+ * ``*_workspace_size`` call reports.  Every call returns a vesper_status;
+ * vesper_last_error() gives a one-line message for the calling thread.
+ *
+ * The reference is a Python program with no FFI; each entry point below
+ * replaces the reference function cited beside it, with the same argument
+ * meaning, and the Python host layer (vesper_python_gb300/vesper.py) keeps
+ * the reference's function names and raises where the reference raises.
+ */
+#ifndef VESPER_GB300_H
+#define VESPER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum vesper_status {
+    VESPER_OK = 0,
+    VESPER_ERR_INVALID = 1,      /* bad argument (null pointer, size, mode)          */
+    VESPER_ERR_UNSUPPORTED = 2,  /* grid side not supported by the kernels           */
+    VESPER_ERR_CUDA = 3,         /* CUDA launch/runtime error                        */
+    VESPER_ERR_WORKSPACE = 4,    /* workspace too small                              */
+    VESPER_ERR_DEVICE = 5        /* a kernel reported an error through its status word */
+};
+
+/* Search modes (main.py:194-203 letters V/O/C/P/L, plus the prob search). */
+enum vesper_mode {
+    VESPER_MODE_VEC = 0,        /* 'V' VecProduct: 3 vector channels               */
+    VESPER_MODE_OVERLAP = 1,    /* 'O' Overlap                                      */
+    VESPER_MODE_CC = 2,         /* 'C' CC                                           */
+    VESPER_MODE_PCC = 3,        /* 'P' PCC                                          */
+    VESPER_MODE_LAPLACIAN = 4,  /* 'L' Laplacian                                    */
+    VESPER_MODE_PROB = 5        /* prob search: 3 vector + 4 probability channels   */
+};
+
+/* Library version (major*10000 + minor*100 + patch). */
+int vesper_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *vesper_last_error(void);
+
+/* Largest grid side ``dim`` the search kernels accept for ``mode``. */
+int vesper_max_dim(int mode);
+
+/* FFT length rule of the grid side: 1 if ``n`` = 2^a 3^b 5^c 7^d 11^e 13^f
+ * with e+f <= 1 (pyFFTW next_fast_len, VESPER_1_prob_new.py:97), else 0. */
+int vesper_fast_len_ok(int n);
+
+/* ---------------------------------------------------------------------------
+ * Map preparation: the threshold and radius of mrc_set_vox_size
+ * (VESPER_1_prob_new.py:72-89).  In place, data[data < th] = 0 (float32
+ * compare; th < 0 acts as 0 and does not shift the data).  out2 is DEVICE
+ * uint64[2]: out2[0] = the bits of the largest squared distance
+ * ((i-cx)^2 + (j-cy)^2) + (k-cz)^2 (float64) of a non-zero voxel from the HOST
+ * centre cent[3] (voxel units, [x][y][z] indexing); out2[1] = the number of
+ * non-zero voxels (0: the reference's max() of an empty list raises).
+ * ------------------------------------------------------------------------- */
+int vesper_prepare_map(float *data, int sx, int sy, int sz, double threshold, const double *cent, uint64_t *out2,
+                       void *stream);
+
+/* fastVEC statistics of a d^3 float64 density (VESPER_1_prob_new.py:157-161):
+ * stats_out DEVICE double[5] = {sum, count != 0, mean of > 0, L2 norm of > 0,
+ * L2 norm of (> 0 values - mean)}. */
+int vesper_map_stats(const double *data, int dim, double *stats_out, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * fastVEC: Gaussian-weighted unit-vector field of one resampled map.
+ * Replaces doFastVEC / calc (VESPER_1_prob_new.py:121-142, :180-257).
+ *
+ *   src        float32 [sx][sy][sz]   thresholded source density
+ *   src_width  source voxel width (A)            src_orig  HOST double[3]
+ *   dim        destination side d                dest_width coarse spacing s
+ *   dest_orig  HOST double[3]                    dreso      bandwidth g
+ *   data_out   double [d][d][d]   Gaussian-weighted density (0 where skipped)
+ *   data_f32   float  [d][d][d]   optional float32 copy of data_out (NULL ok);
+ *              prob mode stores the density as float32 (main.py:345)
+ *   vec_out    float  [d][d][d][3] unit vectors (0 where skipped)
+ * ------------------------------------------------------------------------- */
+int vesper_fastvec_workspace_size(int sx, int sy, int sz, int dim, size_t *bytes);
+int vesper_fastvec(const float *src, int sx, int sy, int sz, double src_width, const double *src_orig,
+                   int dim, double dest_width, const double *dest_orig, double dreso,
+                   double *data_out, float *data_f32, float *vec_out,
+                   void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Rotation of the query map for ``nrot`` rotations.
+ * Replaces rot_mrc (VESPER_1_prob_new.py:279-354) and, with ``probs``,
+ * rot_mrc_prob (:1211-1299).
+ *
+ *   data     double [d][d][d]         vec  float [d][d][d][3]
+ *   probs    float  [4][d][d][d] or NULL (each channel masked by its own != 0)
+ *   rotmats  float  [nrot][3][3]  np.flip of the ZYX Euler matrix with
+ *            |m| < 1e-15 zeroed, cast to float32 (VESPER_1_prob_new.py:305-310)
+ *   data_out double [nrot][d][d][d], vec_out float [nrot][d][d][d][3],
+ *   probs_out float [nrot][4][d][d][d] (only with probs)
+ * ------------------------------------------------------------------------- */
+int vesper_rot_gather(const double *data, const float *vec, const float *probs, int dim,
+                      const float *rotmats, int nrot, double *data_out, float *vec_out, float *probs_out,
+                      void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Target spectra conj(rfftn(x_c)) of the target map's mode fields, computed
+ * in float64 and stored as complex64 [C][d][d][d/2+1] (interleaved re, im).
+ * Replaces the target set-up of search_map_fft (VESPER_1_prob_new.py:601-628)
+ * and search_map_fft_prob (:846-864).  ``ave`` is the target's fastVEC
+ * average (used by PCC).  For VESPER_MODE_PROB ``probs`` holds the four
+ * target probability maps (float32 [4][d][d][d]).
+ * ------------------------------------------------------------------------- */
+int vesper_spectra_bytes(int dim, int mode, size_t *bytes);
+int vesper_target_workspace_size(int dim, int mode, size_t *bytes);
+int vesper_target_spectra(const double *data, const float *vec, const float *probs, int dim, int mode,
+                          double ave, void *spectra_out, void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Rotational search: for every rotation r, rotate the query map, correlate it
+ * with the target over all circular translations by FFT and keep the best
+ * translation (largest score, first in C order).
+ * Replaces the rotation loops of search_map_fft (VESPER_1_prob_new.py:644-655,
+ * :724-736) over rot_and_search_fft (:1418-1459, fft_search_best_dot :464-491,
+ * fft_search_score_trans_1d :529-565, laplacian_filter :494-526,
+ * find_best_trans_list :357-374), and of search_map_fft_prob (:880-896,
+ * :935-962, :1025-1080) over rot_and_search_fft_prob (:1462-1527,
+ * find_best_trans_mixed :1530-1545).
+ *
+ *   spectra   output of vesper_target_spectra for the same dim and mode
+ *   data, vec, probs   the query map (probs only for VESPER_MODE_PROB)
+ *   ave       the TARGET's fastVEC average (PCC query transform, :1447-1450)
+ *   rotmats   float [nrot][3][3] as for vesper_rot_gather
+ *   mix       HOST double[5] {alpha, vstd, vave, pstd, pave} or NULL; only for
+ *             VESPER_MODE_PROB, enabling the mixed z-score (pass 2)
+ *   scores_out float [nrot][nscore] raw best scores (unnormalised correlation,
+ *             before the 1/d^3 and CC/PCC scale factors the host applies)
+ *   lin_out   int32 [nrot][nscore] linear index x*d*d + y*d + z of the best
+ *             translation
+ *   nscore = vesper_search_nscore(mode, mix != NULL): 1 for V/O/C/P/L;
+ *            prob: {vec, prob} without mix, {vec, prob, mixed} with mix.
+ *   batch     rotations resident per pipeline step (0 = library default)
+ * ------------------------------------------------------------------------- */
+int vesper_search_nscore(int mode, int with_mix);
+int vesper_search_workspace_size(int dim, int mode, int batch, int nrot, size_t *bytes);
+int vesper_search(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
+                  int mode, double ave, const float *rotmats, int nrot, const double *mix,
+                  float *scores_out, int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes,
+                  void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Stable top-N: indices of the ``topn`` largest of scores[i*stride]
+ * (i < n), ties to the lower index -- Python's stable
+ * sorted(..., reverse=True)[:N] (VESPER_1_prob_new.py:664, :739, :992, :1082).
+ * idx_out int32 [topn]; entries past n are -1.
+ * ------------------------------------------------------------------------- */
+int vesper_topn(const float *scores, int n, int stride, int topn, int32_t *idx_out, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Final-model scoring in float64.  Replaces get_score
+ * (VESPER_1_prob_new.py:1302-1393), including its ``d2 = where(d2 <= 0, 0,
+ * d1)`` (:1357).
+ *   tdata/tvec: target map; tave/tstd/tstd_norm_ave: its fastVEC statistics
+ *   sdata/svec: rotated query map; trans: HOST int[3] best translation
+ *   result_out double[8] = {Nm, total, cc/(std1*std2), pcc/(pstd1*pstd2),
+ *                           DOT score, ave2, std2, pstd2}
+ *   sco_out double [d][d][d] per-voxel dot products (NULL ok)
+ * ------------------------------------------------------------------------- */
+int vesper_rescore_workspace_size(int dim, size_t *bytes);
+int vesper_rescore(const double *tdata, const float *tvec, double tave, double tstd, double tstd_norm_ave,
+                   const double *sdata, const float *svec, int dim, const int32_t *trans, double *result_out,
+                   double *sco_out, void *workspace, size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VESPER_GB300_H */

@@ -1,0 +1,62 @@
+"""The C-ABI library: it builds, loads, exports every symbol the header
+declares, and its host-only entry points answer without a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from vesper_python_gb300 import _native
+
+HEADER = os.path.join(_native.INCLUDE, "vesper_gb300.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(?:int|const char \*)\s*\*?\s*(vesper_\w+)\s*\(", txt)))
+
+
+def test_header_lists_entry_points():
+    syms = declared_symbols()
+    for s in ("vesper_fastvec", "vesper_rot_gather", "vesper_target_spectra", "vesper_search", "vesper_topn",
+              "vesper_rescore"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _native.load()
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+    # the Python binding covers every declared symbol
+    assert set(declared_symbols()) <= set(_native.SIGNATURES)
+
+
+def test_host_queries_without_gpu():
+    lib = _native.load()
+    assert lib.vesper_version() >= 100
+    for n, ok in ((12, 1), (13, 1), (75, 1), (143, 0), (169, 0), (17, 0), (64, 1), (1, 0)):
+        assert lib.vesper_fast_len_ok(n) == ok, n
+    assert lib.vesper_search_nscore(0, 0) == 1 and lib.vesper_search_nscore(5, 0) == 2
+    assert lib.vesper_search_nscore(5, 1) == 3
+    b = _native.size_query("vesper_search_workspace_size", 75, 0, 8, 24624)
+    # S (8 x 3 channels) + U (8 x 1 group) complex64 spectra + keys
+    assert b >= 8 * 4 * 75 * 75 * 38 * 8 + 24624 * 3 * 8
+    assert _native.size_query("vesper_spectra_bytes", 75, 0) == 3 * 75 * 75 * 38 * 8
+    assert _native.size_query("vesper_fastvec_workspace_size", 200, 200, 200, 75) > 0
+
+
+def test_invalid_arguments_return_status():
+    lib = _native.load()
+    rc = lib.vesper_search(None, None, None, None, 12, 0, 0.0, None, 4, None, None, None, 0, None, 0, None)
+    assert rc == 1
+    assert b"missing" in lib.vesper_last_error()
+    rc = lib.vesper_search(None, None, None, None, 17, 0, 0.0, None, 4, None, None, None, 0, None, 0, None)
+    assert rc == 2  # 17 is not a supported FFT length
+    rc = lib.vesper_topn(None, 10, 1, 3, None, None)
+    assert rc == 1
+    with pytest.raises(_native.VesperError):
+        _native.check(lib.vesper_rot_gather(None, None, None, 12, None, 1, None, None, None, None))
+    rc = lib.vesper_fastvec(None, 1, 1, 1, 1.0, None, 4, 1.0, None, 16.0, None, None, None, None, 0, None)
+    assert rc == 1
+    assert lib.vesper_search_workspace_size(12, 0, 0, 10, ctypes.POINTER(ctypes.c_size_t)()) == 1

@@ -1,0 +1,154 @@
+"""Host-side logic of the package (no GPU): angle grid, rotation matrices,
+refinement set, map I/O and set-up, CLI, output geometry, PDB writer and the
+rotation sharding helpers."""
+import contextlib
+import io
+import os
+
+import numpy as np
+import pytest
+
+from oracle import vesper_oracle as orc
+from vesper_python_gb300 import main as cli
+from vesper_python_gb300 import mrc, shard, synth
+from vesper_python_gb300 import vesper as vg
+
+
+def test_angle_grid_matches_golden(golden_dir):
+    g = np.load(os.path.join(golden_dir, "angles.npz"))
+    for key in g.files:
+        assert np.array_equal(vg.calc_angle_comb(float(key[1:])), g[key])
+
+
+def test_rotation_matrices_bitwise():
+    angles = vg.calc_angle_comb(30.0)
+    mats = vg.rot_matrices(angles)
+    for a, m in zip(angles[::5], mats[::5]):
+        assert np.array_equal(m, orc.rot_matrix_f32(a))
+    ref = orc.refine_angles(angles[[0, 17, 500, 1007]])
+    assert np.array_equal(vg.refine_angle_list(angles[[0, 17, 500, 1007]]), ref)
+    for a, m in zip(ref, vg.rot_matrices(ref)):
+        assert np.array_equal(m, orc.rot_matrix_f32(a))
+
+
+def test_next_fast_len_agrees():
+    for n in range(1, 400):
+        assert vg.next_fast_len(n) == orc.next_fast_len(n)
+
+
+def test_mrc_roundtrip(tmp_path):
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=(7, 5, 6)).astype(np.float32)  # (nz, ny, nx)
+    p = tmp_path / "m.mrc"
+    mrc.write_mrc(p, a, voxel_size=1.5, origin=(1.0, -2.0, 3.5))
+    m = mrc.read_mrc(p)
+    assert (m.nx, m.ny, m.nz) == (6, 5, 7)
+    assert np.array_equal(m.data, a)
+    assert np.array_equal(m.voxel_size, np.float32([1.5, 1.5, 1.5]))
+    assert np.array_equal(m.origin, np.float32([1.0, -2.0, 3.5]))
+    o = vg.mrc_obj(str(p))
+    assert o.data.shape == (6, 5, 7) and np.array_equal(o.data, np.swapaxes(a, 0, 2))
+    assert o.xwidth.dtype == np.float32 and o.orig.dtype == np.float32
+
+
+def test_mrc_bad_files(tmp_path):
+    p = tmp_path / "short.mrc"
+    p.write_bytes(b"\0" * 100)
+    with pytest.raises(mrc.MrcFormatError):
+        mrc.read_mrc(p)
+    a = np.zeros((4, 4, 4), np.float32)
+    q = tmp_path / "trunc.mrc"
+    mrc.write_mrc(q, a)
+    q.write_bytes(q.read_bytes()[:-10])
+    with pytest.raises(mrc.MrcFormatError):
+        mrc.read_mrc(q)
+
+
+def test_set_vox_size_prints_match_reference(golden_dir):
+    pair = synth.workload_pair("pair128_s7_a30", seed=0)
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        m1 = vg.mrc_obj.from_array(pair.map1, 1.0, pair.orig1)
+        m2 = vg.mrc_obj.from_array(pair.map2, 1.0, pair.orig2)
+        _, n1 = vg.mrc_set_vox_size(m1, 0.1, 7.0)
+        _, n2 = vg.mrc_set_vox_size(m2, 0.1, 7.0)
+    ref = open(os.path.join(golden_dir, "search_pair128_setup.txt")).read()
+    assert ref.startswith(buf.getvalue())
+    g = np.load(os.path.join(golden_dir, "search_pair128.npz"))
+    cli._unify(n1, n2, 7.0)
+    assert n1.xdim == int(g["dim"]) and np.array_equal(n1.orig, g["orig1"]) and np.array_equal(n2.orig, g["orig2"])
+
+
+def test_empty_map_raises_like_reference():
+    m = vg.mrc_obj.from_array(np.zeros((8, 8, 8), np.float32))
+    with pytest.raises(ValueError):
+        with contextlib.redirect_stdout(io.StringIO()):
+            vg.mrc_set_vox_size(m, 0.1, 7.0)
+
+
+def test_convert_trans_matches_oracle():
+    cen1 = np.array([64.0, 64.0, 64.0])
+    cen2 = np.array([60.5, 61.0, 59.0])
+    for ang in ([240.0, 90.0, 355.0], [0.0, 0.0, 0.0], [35.0, 125.0, 270.0]):
+        for tr in ((0, 0, 0), (12, 1, 7), (6, 7, 12)):
+            a = vg.convert_trans(cen1, cen2, vg.euler2rot(ang), tr, 7.0, 13)
+            b = orc.convert_trans(cen1, cen2, orc.euler2rot(ang), tr, 7.0, 13)
+            assert np.array_equal(a, b)
+
+
+def test_cli_defaults_and_quirks():
+    p = cli.build_parser()
+    a = p.parse_args(["orig", "-a", "x.mrc", "-b", "y.mrc"])
+    assert (a.t, a.T, a.g, a.s, a.A, a.N, a.S, a.M, a.E, a.o) == (None, None, 16.0, 7.0, 30.0, 10, False, "V", False,
+                                                                  None)
+    a = p.parse_args(["orig", "-a", "x", "-b", "y", "-S", "False", "-A", "15"])
+    assert a.S is True and isinstance(a.A, float)  # type=bool: any non-empty string is True
+    b = p.parse_args(["prob", "-a", "x", "-npa", "p", "-b", "y", "-npb", "q"])
+    assert (b.alpha, b.P, b.vav, b.vstd, b.pav, b.pstd) == (0.5, 4, None, None, None, None)
+    with pytest.raises(SystemExit):
+        with contextlib.redirect_stderr(io.StringIO()):
+            p.parse_args(["orig", "-a", "x"])
+
+
+def test_show_vec_format(tmp_path):
+    rng = np.random.default_rng(1)
+    d = 5
+    data = np.where(rng.random((d, d, d)) < 0.3, rng.uniform(0.5, 2, (d, d, d)), 0.0)
+    vec = rng.normal(size=(d, d, d, 3)).astype(np.float32)
+    sco = rng.normal(size=(d, d, d))
+    vg.show_vec(np.array([1.0, 2.0, 3.0]), vec, data, sco, 12.3456, 7.0, (4, 1, 0), (0, 0, 0), tmp_path, 3)
+    f = tmp_path / "R_03-S__12.346.pdb"
+    lines = f.read_text().splitlines()
+    nz = np.argwhere(data != 0)
+    assert len(lines) == 2 * len(nz)
+    add = np.array([1.0, 2.0, 3.0]) - np.array([-1, 1, 0]) * 7.0
+    x, y, z = nz[0]
+    tmp = np.array([x, y, z]) * 7.0 + add
+    assert lines[0] == "ATOM{:>7d}  CA  ALA{:>6d}    ".format(1, 1) + "{:8.3f}{:8.3f}{:8.3f}{:6.2f}{:6.2f}".format(
+        tmp[0], tmp[1], tmp[2], 1.0, sco[x, y, z])
+    assert lines[1].startswith("ATOM      2  CB  ALA     1    ")
+
+
+def test_shard_merge_equals_global_stable_topn():
+    rng = np.random.default_rng(2)
+    scores = rng.integers(0, 40, 1000).astype(np.float32)  # many exact ties
+    ref = orc.topn(scores, 25)
+    for world in (1, 2, 3, 4, 7):
+        parts = []
+        for r in range(world):
+            lo, hi = shard.shard_range(len(scores), r, world)
+            parts.append(shard.local_topn(scores[lo:hi], 25, lo))
+        _, ix = shard.merge_topn(parts, 25)
+        assert np.array_equal(ix, ref), world
+    assert shard.shard_range(10, 0, 3) == (0, 4) and shard.shard_range(10, 2, 3) == (7, 10)
+
+
+def test_workload_generator_is_deterministic():
+    a = synth.make_pair(5, 32, 20, 10.0)
+    b = synth.make_pair(5, 32, 20, 10.0)
+    assert np.array_equal(a.map1, b.map1) and np.array_equal(a.map2, b.map2)
+    assert a.map1.shape == (32, 32, 32) and a.map2.shape == (16, 16, 16)
+    p = synth.make_pair(5, 32, 20, 10.0, with_prob=True)
+    assert p.prob1.shape == (32, 32, 32, 4)
+    s = p.prob1.sum(-1)
+    assert np.allclose(s[p.map1 >= 0.1], 1.0, atol=1e-5) and np.all(s[p.map1 < 0.1] == 0)

@@ -1,0 +1,150 @@
+"""The CPU oracle against the golden vectors recorded from the unmodified
+reference (tests/golden/make_golden.py).  No GPU needed."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from oracle import vesper_oracle as orc
+
+
+def _g(golden_dir, name):
+    return np.load(os.path.join(golden_dir, name))
+
+
+def digest(*arrays):
+    h = hashlib.sha1()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def test_angle_grids(golden_dir):
+    g = _g(golden_dir, "angles.npz")
+    for key in g.files:
+        a = float(key[1:])
+        assert np.array_equal(orc.calc_angle_comb(a), g[key]), key
+    # row order: z slowest, x middle, y fastest
+    ac = g["A30"]
+    assert tuple(ac[1]) == (0, 30, 0) and tuple(ac[12]) == (30, 0, 0) and tuple(ac[144]) == (0, 0, 30)
+    assert len(g["A10"]) == 24624 and len(g["A15"]) == 7488 and len(ac) == 1008
+
+
+@pytest.mark.parametrize("d", [8, 9, 12, 15])
+def test_rot_mrc_all_rotations(golden_dir, d):
+    g = _g(golden_dir, "rot_small.npz")
+    data, vec = g[f"d{d}_data"], g[f"d{d}_vec"]
+    ang = orc.calc_angle_comb(30.0)
+    dig = g[f"d{d}_digest"]
+    bad = [r for r, a in enumerate(ang) if digest(*orc.rot_mrc(data, vec, a)) != dig[r]]
+    assert not bad
+    for r in (0, 1, 13, 144, 500, 1007):
+        nv, nd = orc.rot_mrc(data, vec, ang[r])
+        assert np.array_equal(nv, g[f"d{d}_r{r}_vec"]) and np.array_equal(nd, g[f"d{d}_r{r}_data"])
+
+
+def test_rot_mrc_fine_and_refinement_angles(golden_dir):
+    g = _g(golden_dir, "rot_small.npz")
+    for d in (12, 15):
+        data, vec = g[f"d{d}_data"], g[f"d{d}_vec"]
+        for a, dg in zip(g["angles10_sub"], g[f"d{d}_a10_digest"]):
+            assert digest(*orc.rot_mrc(data, vec, a)) == dg
+        for a, dg in zip(g["extra_angles"], g[f"d{d}_extra_digest"]):
+            assert digest(*orc.rot_mrc(data, vec, a)) == dg
+
+
+@pytest.mark.parametrize("d", [9, 12])
+def test_rot_mrc_prob(golden_dir, d):
+    g = _g(golden_dir, "rot_small.npz")
+    data, vec, probs = g[f"p{d}_data"], g[f"p{d}_vec"], g[f"p{d}_probs"]
+    ang = orc.calc_angle_comb(30.0)[::11]
+    for a, dg in zip(ang, g[f"p{d}_digest"]):
+        assert digest(*orc.rot_mrc_prob(data, vec, *probs, a)) == dg
+
+
+def test_odd_side_collision_rule():
+    """Odd d: destination index (d-1)/2 takes the later of two source rows and
+    the last plane stays empty (identity rotation)."""
+    d = 15
+    data = np.arange(1, d ** 3 + 1, dtype=np.float64).reshape(d, d, d)
+    vec = np.ones((d, d, d, 3), np.float32)
+    _, nd = orc.rot_mrc(data, vec, (0.0, 0.0, 0.0))
+    assert np.all(nd[14] == 0) and np.all(nd[:, 14] == 0) and np.all(nd[:, :, 14] == 0)
+    assert nd[7, 7, 7] == data[8, 8, 8]
+    assert nd[3, 3, 3] == data[3, 3, 3] and nd[10, 10, 10] == data[11, 11, 11]
+
+
+def test_fastvec_c_restatement(golden_dir):
+    """C restatement of doFastVEC vs the pure-Python reference loop: data within
+    2 ulp-scale (numpy vs libm exp), vectors identical."""
+    g = _g(golden_dir, "fastvec_small.npz")
+    for i in range(3):
+        S, sw, so0, so1, so2, dd, dw, do0, do1, do2, gg = g[f"c{i}_params"]
+        data, vec = orc.fastvec(g[f"c{i}_src"], sw, np.float32([so0, so1, so2]), int(dd), dw, [do0, do1, do2], gg)
+        rd = g[f"c{i}_data"]
+        assert np.array_equal(data != 0, rd != 0)
+        assert np.max(np.abs(data - rd) / np.maximum(np.abs(rd), 1e-300)) < 1e-15
+        assert np.array_equal(vec, g[f"c{i}_vec"])
+        st = np.array(orc.fastvec_stats(data), np.float64)
+        assert np.allclose(st, g[f"c{i}_stats"], rtol=1e-14)
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_search_per_rotation_bit_exact(golden_dir, mode):
+    g = _g(golden_dir, "search_pair128.npz")
+    s1 = g["stats1"]
+    ts = orc.target_spectra(orc.mode_field(mode, g["data1"], g["vec1"], s1[2]))
+    ang = g[f"{mode}_angles"]
+    sc, tr = orc.search(ts, mode, g["data2"], g["vec2"], ang, s1[2])
+    scale = orc.score_scale(mode, s1[3], s1[4])
+    assert np.array_equal(sc.astype(np.float64) * scale, g[f"{mode}_score"])
+    assert np.array_equal(tr, g[f"{mode}_trans"])
+    R = len(orc.calc_angle_comb(30.0))
+    top = orc.topn(sc[:R], 10)
+    assert np.array_equal(orc.refine_angles(ang[top]), ang[R:])
+    rtop = orc.topn(sc[R:], 10)
+    assert np.array_equal(ang[R:][rtop], g[f"{mode}_refined_angle"])
+    assert np.array_equal(tr[R:][rtop], g[f"{mode}_refined_trans"])
+
+
+def test_set_vox_size_matches_reference_prints(golden_dir):
+    from vesper_python_gb300 import synth
+    g = _g(golden_dir, "search_pair128.npz")
+    pair = synth.workload_pair("pair128_s7_a30", seed=0)
+    m1 = orc.OMap(pair.map1, 1.0, pair.orig1)
+    m2 = orc.OMap(pair.map2, 1.0, pair.orig2)
+    d1, o1, c1, _ = orc.set_vox_size(m1, 0.1, 7.0)
+    d2, o2, c2, _ = orc.set_vox_size(m2, 0.1, 7.0)
+    dim, o1, o2 = orc.unify(d1, o1, c1, d2, o2, c2, 7.0)
+    assert dim == int(g["dim"])
+    assert np.array_equal(o1, g["orig1"]) and np.array_equal(o2, g["orig2"])
+    data1, vec1 = orc.fastvec(m1.data, np.float64(m1.xwidth), m1.orig.astype(np.float64), dim, 7.0, o1, 16.0)
+    assert np.array_equal(data1, g["data1"]) and np.array_equal(vec1, g["vec1"])
+    txt = open(os.path.join(golden_dir, "search_pair128_setup.txt")).read()
+    assert "Nvox= 12, 12, 12" in txt and "Nvox= 13, 13, 13" in txt
+
+
+def test_prob_passes(golden_dir):
+    g = _g(golden_dir, "prob_pair128.npz")
+    d = int(g["dim"])
+    tspec = orc.target_spectra([g["vec1"][..., 0], g["vec1"][..., 1], g["vec1"][..., 2]] + list(g["probs1"]))
+    ang = orc.calc_angle_comb(30.0)[::9]
+    idx = np.arange(0, 1008, 9)
+    for a, r in zip(ang, idx):
+        vs, vt, ps, pt, _, _ = orc.rot_and_search_prob(tspec, g["data2"], g["vec2"], g["probs2"], a, 0.5)
+        assert np.float64(vs) == g["pass1_vscore"][r] and tuple(vt) == tuple(g["pass1_vtrans"][r])
+        assert np.float64(ps) == g["pass1_pscore"][r] and tuple(pt) == tuple(g["pass1_ptrans"][r])
+    st = orc.prob_stats(g["pass1_vscore"], g["pass1_pscore"], 1.0 / d ** 3)
+    for a, r in zip(ang, idx):
+        res = orc.rot_and_search_prob(tspec, g["data2"], g["vec2"], g["probs2"], a, 0.5, st, promotion="numpy2")
+        assert np.float64(res[4]) == g["pass2_mscore"][r] and tuple(res[5]) == tuple(g["pass2_mtrans"][r])
+    txt = open(os.path.join(golden_dir, "prob_pair128.txt")).read()
+    assert f"DotScore Std= {float(st[0])!r} DotScore Ave= {float(st[1])!r}" in txt
+
+
+def test_next_fast_len():
+    assert [orc.next_fast_len(n) for n in (1, 2, 11, 13, 17, 19, 23, 29, 37, 74, 97, 143, 169)] == \
+        [1, 2, 11, 13, 18, 20, 24, 30, 39, 75, 98, 144, 175]
+    # 11*13 and 13*13 need e+f = 2 -> skipped
+    assert orc.next_fast_len(143) == 144

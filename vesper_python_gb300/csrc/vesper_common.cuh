@@ -1,0 +1,128 @@
+// Shared host/device helpers of the VESPER GB300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+
+#include "vesper_fft.cuh"
+#include "../../include/vesper_gb300.h"
+
+namespace vg {
+
+// ---- error reporting (per host thread) --------------------------------------
+void set_error(const char *fmt, ...);
+int fail(int code, const char *fmt, ...);
+int cuda_check(const char *what);
+
+#define VG_CHECK_LAUNCH(what)                          \
+    do {                                               \
+        int _rc = ::vg::cuda_check(what);              \
+        if (_rc != VESPER_OK) return _rc;              \
+    } while (0)
+
+// ---- FFT plans ----------------------------------------------------------------
+// Factor n into supported radices (4s first, then 2, 3, 5, 7, 11, 13).  Returns
+// false when n has another prime factor or more than one of 11 and 13.
+bool make_plan(int n, FftPlan *plan);
+
+// ---- workspace carving ----------------------------------------------------------
+struct Carver {
+    char *base;
+    size_t cap, off;
+    __host__ Carver(void *b, size_t c) : base((char *)b), cap(c), off(0) {}
+    template <typename T>
+    __host__ T *take(size_t count) {
+        off = (off + 255) & ~(size_t)255;
+        T *p = (T *)(base ? base + off : nullptr);
+        off += count * sizeof(T);
+        return p;
+    }
+    __host__ bool ok() const { return off <= cap; }
+};
+
+// ---- ordering key for (score desc, index asc) ---------------------------------
+__device__ __forceinline__ uint32_t float_order(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float order_float(uint32_t o) {
+    const uint32_t u = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+    return __uint_as_float(u);
+}
+__device__ __forceinline__ unsigned long long make_key(float s, uint32_t lin) {
+    return ((unsigned long long)float_order(s) << 32) | (unsigned long long)(0xffffffffu - lin);
+}
+
+// ---- reference gather geometry (rot_mrc, VESPER_1_prob_new.py:279-354) --------
+// Candidate source new_pos indices i (per axis) that land on destination t
+// after dest = int(trunc(i - d/2) + d/2), in descending order of i.  For
+// even d only i = t; for odd d (m = (d-1)/2) i = t below m, {m+1, m} at m,
+// t+1 above m and none at d-1.
+__device__ __forceinline__ int gather_cands(int t, int d, int *c) {
+    if ((d & 1) == 0) { c[0] = t; return 1; }
+    const int m = (d - 1) >> 1;
+    if (t < m) { c[0] = t; return 1; }
+    if (t == m) { c[0] = m + 1; c[1] = m; return 2; }
+    if (t < d - 1) { c[0] = t + 1; return 1; }
+    return 0;
+}
+
+// old position of the new_pos row (ix, iy, iz): float32 sgemm order with an
+// FMA chain over k = 0, 1, 2, then a float32 add of d/2.  F is np.flip(mtx).
+__device__ __forceinline__ bool old_index(const float *F, int d, float cf, float hx, float hy, float hz,
+                                          int &ox, int &oy, int &oz) {
+    float o[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float acc = __fmul_rn(hx, F[a * 3 + 0]);
+        acc = __fmaf_rn(hy, F[a * 3 + 1], acc);
+        acc = __fmaf_rn(hz, F[a * 3 + 2], acc);
+        o[a] = __fadd_rn(acc, cf);
+    }
+    const float df = (float)d;
+    if (!(o[0] >= 0.f && o[1] >= 0.f && o[2] >= 0.f && o[0] < df && o[1] < df && o[2] < df)) return false;
+    ox = (int)o[0];
+    oy = (int)o[1];
+    oz = (int)o[2];
+    return true;
+}
+
+// Winning source voxel for destination (x, y, z): the last reference row
+// (z slowest, x middle, y fastest) whose old position is in bounds and passes
+// ``mask``.  Returns the source linear index or -1.
+template <class Mask>
+__device__ __forceinline__ int gather_src(const float *F, int d, int x, int y, int z, Mask mask) {
+    int cx[2], cy[2], cz[2];
+    const int nx = gather_cands(x, d, cx), ny = gather_cands(y, d, cy), nz = gather_cands(z, d, cz);
+    const float cf = 0.5f * (float)d;
+    const float hc = 0.5f * (float)d;
+    for (int a = 0; a < nz; ++a) {
+        const float hz = (float)cz[a] - hc;
+        for (int b = 0; b < nx; ++b) {
+            const float hx = (float)cx[b] - hc;
+            for (int e = 0; e < ny; ++e) {
+                const float hy = (float)cy[e] - hc;
+                int ox, oy, oz;
+                if (!old_index(F, d, cf, hx, hy, hz, ox, oy, oz)) continue;
+                const int src = (ox * d + oy) * d + oz;
+                if (mask(src)) return src;
+            }
+        }
+    }
+    return -1;
+}
+
+// rotated vector: new_vec_j = sum_k v_k F[k][j] (sgemm order, FMA chain)
+__device__ __forceinline__ void rotate_vec(const float *F, float v0, float v1, float v2, float *o) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        float acc = __fmul_rn(v0, F[0 * 3 + j]);
+        acc = __fmaf_rn(v1, F[1 * 3 + j], acc);
+        o[j] = __fmaf_rn(v2, F[2 * 3 + j], acc);
+    }
+}
+
+}  // namespace vg

@@ -1,0 +1,66 @@
+// Library-wide host helpers: error reporting, FFT plans, small queries.
+#include <cstring>
+#include <string>
+
+#include "vesper_common.cuh"
+
+namespace vg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_check(const char *what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(VESPER_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return VESPER_OK;
+}
+
+bool make_plan(int n, FftPlan *plan) {
+    if (n < 1) return false;
+    int rad[64], k = 0, m = n;
+    while (m % 4 == 0) { rad[k++] = 4; m /= 4; }
+    while (m % 2 == 0) { rad[k++] = 2; m /= 2; }
+    int big = 0;
+    const int primes[] = {3, 5, 7, 11, 13};
+    for (int p : primes)
+        while (m % p == 0) {
+            if (p >= 11) ++big;
+            rad[k++] = p;
+            m /= p;
+        }
+    if (m != 1 || big > 1 || k > kMaxStages) return false;
+    plan->n = n;
+    plan->nst = k;
+    for (int i = 0; i < k; ++i) plan->rad[i] = rad[i];
+    if (n == 1) { plan->nst = 0; }
+    return true;
+}
+
+}  // namespace vg
+
+extern "C" int vesper_version(void) { return 100; }
+
+extern "C" const char *vesper_last_error(void) { return vg::g_last_error.c_str(); }
+
+extern "C" int vesper_fast_len_ok(int n) {
+    vg::FftPlan p;
+    return (n >= 2 && vg::make_plan(n, &p)) ? 1 : 0;
+}

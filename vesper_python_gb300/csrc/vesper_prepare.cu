@@ -1,0 +1,122 @@
+// Map preparation on the device: the threshold and maximum radius of
+// mrc_set_vox_size (VESPER_1_prob_new.py:72-89) and the fastVEC statistics
+// (VESPER_1_prob_new.py:157-161).
+#include <algorithm>
+
+#include "vesper_common.cuh"
+
+namespace vg {
+
+// data[data < th] = 0 (float32 compare), and the largest squared distance
+// ((i-cx)^2 + (j-cy)^2) + (k-cz)^2 of a non-zero voxel, as the bits of a
+// non-negative double (ordered like unsigned integers) via atomicMax.
+__global__ void k_prepare(float *data, int sx, int sy, int sz, float th, double cx, double cy, double cz,
+                          unsigned long long *out) {
+    const size_t n = (size_t)sx * sy * sz;
+    double best = -1.0;
+    unsigned long long cnt = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float v = data[i];
+        if (v < th) {
+            v = 0.f;
+            data[i] = 0.f;
+        }
+        if (v != 0.f) {
+            const int k = (int)(i % sz), j = (int)((i / sz) % sy), x = (int)(i / ((size_t)sy * sz));
+            const double a = (double)x - cx, b = (double)j - cy, c = (double)k - cz;
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+            best = d2 > best ? d2 : best;
+            ++cnt;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_down_sync(0xffffffffu, best, o);
+        best = w > best ? w : best;
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0 && cnt > 0) {
+        atomicMax(&out[0], (unsigned long long)__double_as_longlong(best));
+        atomicAdd(&out[1], cnt);
+    }
+}
+
+__global__ void k_init_u64(unsigned long long *p) {
+    p[0] = 0ull;
+    p[1] = 0ull;
+}
+
+// fastVEC statistics in float64, one block: dsum, Nact, ave, std, std_norm_ave.
+constexpr int kStThreads = 1024;
+__device__ __forceinline__ double st_block_sum(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        red[32] = s;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+__global__ void __launch_bounds__(kStThreads) k_stats(const double *data, size_t n, double *out) {
+    __shared__ double red[33];
+    double s = 0.0, cnt = 0.0, pos = 0.0, q = 0.0, np_ = 0.0;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = data[i];
+        s += v;
+        if (v != 0.0) cnt += 1.0;
+        if (v > 0.0) {
+            pos += v;
+            q += v * v;
+            np_ += 1.0;
+        }
+    }
+    s = st_block_sum(s, red);
+    cnt = st_block_sum(cnt, red);
+    pos = st_block_sum(pos, red);
+    q = st_block_sum(q, red);
+    np_ = st_block_sum(np_, red);
+    const double ave = pos / np_;
+    double p2 = 0.0;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = data[i];
+        if (v > 0.0) p2 += (v - ave) * (v - ave);
+    }
+    p2 = st_block_sum(p2, red);
+    if (threadIdx.x == 0) {
+        out[0] = s;
+        out[1] = cnt;
+        out[2] = ave;
+        out[3] = sqrt(q);
+        out[4] = sqrt(p2);
+    }
+}
+
+}  // namespace vg
+
+using namespace vg;
+
+extern "C" int vesper_prepare_map(float *data, int sx, int sy, int sz, double threshold, const double *cent,
+                                  uint64_t *out2, void *stream) {
+    if (!data || !cent || !out2 || sx < 1 || sy < 1 || sz < 1)
+        return fail(VESPER_ERR_INVALID, "vesper_prepare_map: bad arguments");
+    const double th = threshold < 0 ? 0.0 : threshold;   // th < 0 leaves data unshifted (:73-79)
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned long long *acc = (unsigned long long *)out2;
+    k_init_u64<<<1, 1, 0, st>>>(acc);
+    const size_t n = (size_t)sx * sy * sz;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    k_prepare<<<blocks, 256, 0, st>>>(data, sx, sy, sz, (float)th, cent[0], cent[1], cent[2], acc);
+    VG_CHECK_LAUNCH("k_prepare");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_map_stats(const double *data, int dim, double *stats_out, void *stream) {
+    if (!data || !stats_out || dim < 1) return fail(VESPER_ERR_INVALID, "vesper_map_stats: bad arguments");
+    k_stats<<<1, kStThreads, 0, (cudaStream_t)stream>>>(data, (size_t)dim * dim * dim, stats_out);
+    VG_CHECK_LAUNCH("k_stats");
+    return VESPER_OK;
+}
