@@ -1,0 +1,348 @@
+"""Benchmark: map-pair alignments per second on GB300.
+
+One step = one full alignment of a map pair with ``main.py orig`` semantics
+(threshold + grid sizing, fastVEC of both maps, target spectra, search over
+every rotation of the angle grid, top-N, +-5 degree refinement, rotated top-N
+models and their float64 scores) on seeded synthetic maps with the shapes of
+the workload named below.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+``value``: device-resident maps, K steps timed with CUDA events between a
+barrier + synchronize on both sides, whole-job alignments/s (max over ranks).
+``e2e``: the same step through ``Aligner.align_host`` with the maps copied
+from pinned host memory every step and the results read back.
+``--impl reference``: the reference algorithm's CPU path on this host's cores
+(the oracle restatement: C fastVEC with OpenMP, numpy/scipy FFT search with
+every core), timed on a bounded sample of the same workload and scaled to a
+full alignment.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "pair200_s2_a10"
+METRIC = "map-pair alignments/s: learned-proposal vs exhaustive on GPU at ≥99% top-1 match"
+UNIT = "alignments/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--mode", default="V", choices=list("VOCPL"))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def pass_model(dim, mode):
+    """Algorithmic work of each search pass for one rotation (V: 3 channels).
+    FLOPs: a 3-D real FFT of N points is 2.5 N log2 N, split evenly over the
+    three axes; the spectrum product is 8 flops per channel and half-spectrum
+    element.  Bytes: what each pass must read and write in global memory."""
+    N = dim ** 3
+    H = dim // 2 + 1
+    Nh = dim * dim * H
+    C = {"V": 3, "prob": 7}.get(mode, 1)
+    G = 2 if mode == "prob" else 1
+    axis = 2.5 * N * np.log2(dim)          # one axis of one real 3-D FFT
+    return {
+        "query_zy": {"flop": C * 2 * axis, "bytes": N * 20 + C * Nh * 8},
+        "x_corr": {"flop": C * axis + 8 * C * Nh + G * axis, "bytes": C * Nh * 8 * 2 + G * Nh * 8},
+        "inv_argmax": {"flop": G * 2 * axis + N, "bytes": G * Nh * 8},
+    }
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    from vesper_python_gb300 import align, synth
+    from vesper_python_gb300 import vesper as vg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = synth.WORKLOADS[args.workload]
+    mode = {"V": "VecProduct", "O": "Overlap", "C": "CC", "P": "PCC", "L": "Laplacian"}[args.mode]
+    p = align.AlignParams(t=w["t"], T=w["T"], g=w["g"], s=w["s"], A=w["A"], N=w["N"], mode=mode, batch=args.batch)
+    pair = synth.workload_pair(args.workload, seed=rank)   # weak scaling: one pair per rank
+    dev = vg.Device(f"cuda:{local}")
+    al = align.Aligner(dev)
+    src1 = dev.to_dev(pair.map1)
+    src2 = dev.to_dev(pair.map2)
+    h1 = torch.from_numpy(pair.map1).pin_memory()
+    h2 = torch.from_numpy(pair.map2).pin_memory()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev.device)   # > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def maxr(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev.device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(args.warmup):
+        res = al.align_device(src1, src2, pair.width, pair.width, pair.orig1, pair.orig2, p)
+    barrier()
+    # ---- timed region: device-resident inputs --------------------------------
+    clk = ClockSampler(local)
+    clk.start()
+    launches = 0
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        flush.zero_()
+        res = al.align_device(src1, src2, pair.width, pair.width, pair.orig1, pair.orig2, p)
+        launches += al.launches
+    e1.record()
+    barrier()
+    clocks = clk.stop()
+    ms = maxr(e0.elapsed_time(e1))
+    value = world * args.steps / (ms / 1e3)
+    # ---- per-pass device time of the search, one more step with events around
+    # every search launch (kept out of the timed region: the events cost ~10%)
+    prof = {}
+    al.profile = prof
+    flush.zero_()
+    al.align_device(src1, src2, pair.width, pair.width, pair.orig1, pair.orig2, p)
+    barrier()
+    al.profile = None
+    # ---- end to end: host maps copied in every step -------------------------
+    for _ in range(1):
+        al.align_host(None, None, pair.width, pair.width, pair.orig1, pair.orig2, p, pinned=(h1, h2))
+    barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    d2h = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        al.align_host(None, None, pair.width, pair.width, pair.orig1, pair.orig2, p, pinned=(h1, h2))
+        d2h += al.d2h_bytes
+    t1.record()
+    barrier()
+    e2e_ms = maxr(t0.elapsed_time(t1))
+    e2e_value = world * args.steps / (e2e_ms / 1e3)
+    dim = res.dim
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    # ---- roofline of the dominant kernel -------------------------------------
+    pm = pass_model(dim, args.mode if args.mode != "V" else "V")
+    names = ["query_zy", "x_corr", "inv_argmax"]
+    pass_ms = prof["pass_ms"][:3]
+    pass_n = prof["pass_launches"][:3]
+    top = int(np.argmax(pass_ms))
+    nrot_total = len(vg.calc_angle_comb(p.A))
+    per_launch_rot = nrot_total / pass_n[top]
+    avg_s = pass_ms[top] / pass_n[top] / 1e3
+    peak, peak_kind = peaks()
+    ach_bytes = pm[names[top]]["bytes"] * per_launch_rot / avg_s / 1e9
+    ach_flop = pm[names[top]]["flop"] * per_launch_rot / avg_s / 1e12
+    sm_mhz = clocks.get("sm_mhz") or 1900.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "search_traffic.json")
+    if os.path.exists(tr_path):
+        try:
+            traffic = json.load(open(tr_path)).get(names[top])
+        except (OSError, ValueError):
+            traffic = None
+    search_ms = sum(prof["pass_ms"])
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 fastVEC, target spectra, rescoring)",
+        "data": "synthetic (seeded blob maps, 200^3 and 100^3 at 1 A)",
+        "config": {"workload": f"{args.workload}: map1 200^3, map2 100^3, s=2, A=10 (24624 rotations + refinement), "
+                               f"g=16, N=10, mode {args.mode}, exhaustive search",
+                   "grid_side": dim, "rotations": len(vg.calc_angle_comb(p.A)),
+                   "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e_value, 4), "unit": UNIT,
+                "h2d_bytes_per_step": int(h1.numel() * 4 + h2.numel() * 4),
+                "d2h_bytes_per_step": int(d2h / args.steps)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": f"k_{names[top]}", "achieved": round(ach_bytes, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(ach_bytes / peak, 4), "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "fp32": {"achieved_tflops": round(ach_flop, 3), "peak_tflops": round(fp32_peak, 1),
+                              "frac": round(ach_flop / fp32_peak, 4)}},
+        "search_ms_profiled_step": round(search_ms, 3),
+        "pass_ms_profiled_step": [round(x, 3) for x in prof["pass_ms"]],
+        "clocks": clocks,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, threads=1, budget_s=12.0)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(args, threads, budget_s):
+    """The reference algorithm on this host's CPU (the oracle restatement),
+    timed on a bounded sample and scaled to one full alignment."""
+    from oracle import vesper_oracle as orc
+    from vesper_python_gb300 import synth
+    w = synth.WORKLOADS[args.workload]
+    pair = synth.workload_pair(args.workload, seed=0)
+    m1 = orc.OMap(pair.map1, 1.0, pair.orig1)
+    m2 = orc.OMap(pair.map2, 1.0, pair.orig2)
+    d1, o1, c1, _ = orc.set_vox_size(m1, w["t"], w["s"])
+    d2, o2, c2, _ = orc.set_vox_size(m2, w["T"], w["s"])
+    dim, o1, o2 = orc.unify(d1, o1, c1, d2, o2, c2, w["s"])
+    rng = np.random.default_rng(0)
+    nvox = dim ** 3
+    nsamp = 600 if threads == 1 else 600 * threads
+    # fastVEC sample: random destination voxels of both maps
+    t_fv = 0.0
+    for m, o in ((m1, o1), (m2, o2)):
+        idx = rng.choice(nvox, size=min(nsamp, nvox), replace=False)
+        t0 = time.perf_counter()
+        orc.fastvec(m.data, np.float64(m.xwidth), m.orig.astype(np.float64), dim, w["s"], o, w["g"], idx=idx,
+                    nthreads=threads)
+        t_fv += (time.perf_counter() - t0) * nvox / len(idx)
+    # search sample: the rotation loop on real fields
+    data1, vec1 = orc.fastvec(m1.data, np.float64(m1.xwidth), m1.orig.astype(np.float64), dim, w["s"], o1, w["g"],
+                              idx=np.arange(0), nthreads=threads)
+    rngv = np.random.default_rng(1)
+    vec1 = rngv.normal(size=vec1.shape).astype(np.float32)
+    data2 = np.where(rngv.random((dim,) * 3) < 0.3, rngv.uniform(0.5, 2, (dim,) * 3), 0.0)
+    vec2 = rngv.normal(size=vec1.shape).astype(np.float32)
+    ts = orc.target_spectra(orc.mode_field("V", data1, vec1))
+    angles = orc.calc_angle_comb(w["A"])
+    R = len(angles) + 10 * 27
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        orc.rot_and_search(ts, "V", data2, vec2, angles[n * 997 % len(angles)], 0.0, workers=threads)
+        n += 1
+        if time.perf_counter() - t0 > budget_s * 0.5 or n >= 200:
+            break
+    t_rot = (time.perf_counter() - t0) / n
+    total = t_fv + R * t_rot
+    return {"value": round(1.0 / total, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"fastVEC on {nsamp} random voxels per map (scaled to {nvox}), search on {n} rotations "
+                      f"(scaled to {R}); {t_fv:.1f} s fastVEC + {R * t_rot:.1f} s search per alignment",
+            "seconds_per_alignment": round(total, 2)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(args, threads=threads, budget_s=4.0)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / v, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (CPU)",
+            "data": "synthetic (seeded blob maps, 200^3 and 100^3 at 1 A)",
+            "config": {"workload": f"{args.workload}: map1 200^3, map2 100^3, s=2, A=10, mode {args.mode}, "
+                                   f"CPU restatement of the reference path"},
+            "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": cb["sample"]},
+            "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)

@@ -154,6 +154,18 @@ int vesper_search(const void *spectra, const double *data, const float *vec, con
                   float *scores_out, int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes,
                   void *stream);
 
+/* Profiling form of vesper_search, for benchmarks: the same work, plus CUDA
+ * events around every launch.  pass_ms HOST float[4] receives the summed
+ * device time of the rotate+z+y passes, the x/correlation passes, the
+ * inverse y+z/argmax passes and the final decode; pass_launches HOST int[4]
+ * the number of launches of each.  Waits on events up to 16 batches behind
+ * the launch front and at the end, so it returns with the stream drained.
+ * Not re-entrant: one profiling call at a time per process. */
+int vesper_search_profile(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
+                          int mode, double ave, const float *rotmats, int nrot, const double *mix,
+                          float *scores_out, int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes,
+                          void *stream, float *pass_ms, int *pass_launches);
+
 /* ---------------------------------------------------------------------------
  * Stable top-N: indices of the ``topn`` largest of scores[i*stride]
  * (i < n), ties to the lower index -- Python's stable

@@ -314,20 +314,22 @@ def target_spectra(fields):
     return [np.conj(np.fft.rfftn(np.asarray(f, np.float64))) for f in fields]
 
 
-def correlate(target_list, query_list, fp64=False):
+def correlate(target_list, query_list, fp64=False, workers=None):
     """fft_search_best_dot (VESPER_1_prob_new.py:464-491): per channel the
-    unnormalised inverse of (target * rfftn_f32(query)) -> float32 volumes."""
+    unnormalised inverse of (target * rfftn_f32(query)) -> float32 volumes.
+    ``workers`` is scipy.fft's thread count (the reference's FFTW plans use
+    every CPU, VESPER_1_prob_new.py:15)."""
     out = []
     for T, q in zip(target_list, query_list):
         shape = q.shape
         if fp64:
-            Q = scipy.fft.rfftn(np.asarray(q, np.float64))
-            r = scipy.fft.irfftn(T * Q, s=shape) * np.prod(shape)
+            Q = scipy.fft.rfftn(np.asarray(q, np.float64), workers=workers)
+            r = scipy.fft.irfftn(T * Q, s=shape, workers=workers) * np.prod(shape)
             out.append(r)
         else:
-            Q = scipy.fft.rfftn(np.asarray(q, np.float32)).astype(np.complex128)
+            Q = scipy.fft.rfftn(np.asarray(q, np.float32), workers=workers).astype(np.complex128)
             P = (T * Q).astype(np.complex64)
-            r = (scipy.fft.irfftn(P, s=shape) * np.float32(np.prod(shape))).astype(np.float32)
+            r = (scipy.fft.irfftn(P, s=shape, workers=workers) * np.float32(np.prod(shape))).astype(np.float32)
             out.append(r)
     return out
 
@@ -371,21 +373,21 @@ def score_scale(mode, target_std, target_std_norm_ave):
     return 1.0
 
 
-def rot_and_search(tgt_spec, mode, qdata, qvec, angle, target_ave, fp64=False):
+def rot_and_search(tgt_spec, mode, qdata, qvec, angle, target_ave, fp64=False, workers=None):
     """rot_and_search_fft (VESPER_1_prob_new.py:1418-1459) without the CC/PCC
     scale: returns (raw float32 score, (i, j, k), new_vec, new_data)."""
     new_vec, new_data = rot_mrc(qdata, qvec, angle)
     q = mode_field(mode, new_data, new_vec, target_ave)
-    best, trans = best_trans(correlate(tgt_spec, q, fp64=fp64))
+    best, trans = best_trans(correlate(tgt_spec, q, fp64=fp64, workers=workers))
     return best, tuple(int(t) for t in trans), new_vec, new_data
 
 
-def search(tgt_spec, mode, qdata, qvec, angles, target_ave, fp64=False):
+def search(tgt_spec, mode, qdata, qvec, angles, target_ave, fp64=False, workers=None):
     """Per-rotation (raw score, trans) over ``angles``."""
     sc = np.zeros(len(angles), np.float64 if fp64 else np.float32)
     tr = np.zeros((len(angles), 3), np.int64)
     for r, ang in enumerate(angles):
-        s, t, _, _ = rot_and_search(tgt_spec, mode, qdata, qvec, ang, target_ave, fp64=fp64)
+        s, t, _, _ = rot_and_search(tgt_spec, mode, qdata, qvec, ang, target_ave, fp64=fp64, workers=workers)
         sc[r] = s
         tr[r] = t
     return sc, tr

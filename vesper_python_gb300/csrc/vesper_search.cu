@@ -651,10 +651,20 @@ extern "C" int vesper_search_workspace_size(int dim, int mode, int batch, int nr
     return VESPER_OK;
 }
 
-extern "C" int vesper_search(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
-                             int mode, double ave, const float *rotmats, int nrot, const double *mix,
-                             float *scores_out, int32_t *lin_out, int batch, void *workspace,
-                             size_t workspace_bytes, void *stream) {
+// Per-pass event timing of one search (profiling entry point).
+// A ring of event sets keeps kRing batches in flight: a slot's events are read
+// (and its times accumulated) only when the slot is reused or at the end.
+constexpr int kRing = 16;
+struct PassTimer {
+    cudaEvent_t ev[kRing][4][2];
+    bool used[kRing][4];
+    float ms[4];
+};
+
+static int search_impl(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
+                       int mode, double ave, const float *rotmats, int nrot, const double *mix, float *scores_out,
+                       int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes, void *stream,
+                       PassTimer *tm) {
     FftPlan P;
     int rc = check_dim(dim, mode, &P);
     if (rc) return rc;
@@ -708,11 +718,29 @@ extern "C" int vesper_search(const void *spectra, const double *data, const floa
     allow_smem(k_inv_argmax<2>, sc);
     allow_smem(k_inv_argmax<3>, sc);
     const int nbx = (dim * H + W - 1) / W;
+    int slot = 0;
+    auto drain = [&](int sl) {
+        for (int p = 0; p < 4; ++p) {
+            if (!tm->used[sl][p]) continue;
+            cudaEventSynchronize(tm->ev[sl][p][1]);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, tm->ev[sl][p][0], tm->ev[sl][p][1]);
+            tm->ms[p] += ms;
+            tm->used[sl][p] = false;
+        }
+    };
+    auto mark = [&](int pass, int edge) {
+        if (!tm) return;
+        if (edge == 0 && tm->used[slot][pass]) drain(slot);
+        cudaEventRecord(tm->ev[slot][pass][edge], st);
+        if (edge == 1) tm->used[slot][pass] = true;
+    };
     for (int r0 = 0; r0 < nrot; r0 += batch) {
         const int nb = std::min(batch, nrot - r0);
         pa.r0 = r0;
         pc.r0 = r0;
         const dim3 gplane(dim, nb);
+        mark(0, 0);
         switch (mode) {
             case VESPER_MODE_VEC: k_query_zy<VESPER_MODE_VEC><<<gplane, kThreads, sa, st>>>(pa); break;
             case VESPER_MODE_OVERLAP: k_query_zy<VESPER_MODE_OVERLAP><<<gplane, kThreads, sa, st>>>(pa); break;
@@ -722,19 +750,66 @@ extern "C" int vesper_search(const void *spectra, const double *data, const floa
             case VESPER_MODE_PROB: k_query_zy<VESPER_MODE_PROB><<<gplane, kThreads, sa, st>>>(pa); break;
         }
         VG_CHECK_LAUNCH("k_query_zy");
+        mark(0, 1);
+        mark(1, 0);
         k_x_corr<<<dim3(nbx, nb), kThreads, sb, st>>>(pb);
         VG_CHECK_LAUNCH("k_x_corr");
+        mark(1, 1);
+        mark(2, 0);
         switch (nscore) {
             case 1: k_inv_argmax<1><<<gplane, kThreads, sc, st>>>(pc); break;
             case 2: k_inv_argmax<2><<<gplane, kThreads, sc, st>>>(pc); break;
             default: k_inv_argmax<3><<<gplane, kThreads, sc, st>>>(pc); break;
         }
         VG_CHECK_LAUNCH("k_inv_argmax");
+        mark(2, 1);
+        slot = (slot + 1) % kRing;
     }
     const int n = nrot * nscore;
+    mark(3, 0);
     k_decode<<<(n + 255) / 256, 256, 0, st>>>(keys, n, scores_out, lin_out);
     VG_CHECK_LAUNCH("k_decode");
+    mark(3, 1);
+    if (tm)
+        for (int sl = 0; sl < kRing; ++sl) drain(sl);
     return VESPER_OK;
+}
+
+extern "C" int vesper_search(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
+                             int mode, double ave, const float *rotmats, int nrot, const double *mix,
+                             float *scores_out, int32_t *lin_out, int batch, void *workspace,
+                             size_t workspace_bytes, void *stream) {
+    return search_impl(spectra, data, vec, probs, dim, mode, ave, rotmats, nrot, mix, scores_out, lin_out, batch,
+                       workspace, workspace_bytes, stream, nullptr);
+}
+
+extern "C" int vesper_search_profile(const void *spectra, const double *data, const float *vec, const float *probs,
+                                     int dim, int mode, double ave, const float *rotmats, int nrot,
+                                     const double *mix, float *scores_out, int32_t *lin_out, int batch,
+                                     void *workspace, size_t workspace_bytes, void *stream, float *pass_ms,
+                                     int *pass_launches) {
+    if (!pass_ms || !pass_launches) return fail(VESPER_ERR_INVALID, "vesper_search_profile: NULL timing outputs");
+    static PassTimer tm;   // one profiling call at a time per process
+    static bool created = false;
+    if (!created) {
+        for (int sl = 0; sl < kRing; ++sl)
+            for (int p = 0; p < 4; ++p)
+                for (int e = 0; e < 2; ++e)
+                    if (cudaEventCreate(&tm.ev[sl][p][e]) != cudaSuccess)
+                        return fail(VESPER_ERR_CUDA, "vesper_search_profile: cudaEventCreate failed");
+        created = true;
+    }
+    for (int sl = 0; sl < kRing; ++sl)
+        for (int p = 0; p < 4; ++p) tm.used[sl][p] = false;
+    for (int p = 0; p < 4; ++p) tm.ms[p] = 0.f;
+    const int rc = search_impl(spectra, data, vec, probs, dim, mode, ave, rotmats, nrot, mix, scores_out, lin_out,
+                               batch, workspace, workspace_bytes, stream, &tm);
+    for (int p = 0; p < 4; ++p) pass_ms[p] = tm.ms[p];
+    if (batch <= 0) batch = default_batch(dim, mode);
+    const int nb = nrot > 0 ? (nrot + batch - 1) / batch : 0;
+    pass_launches[0] = pass_launches[1] = pass_launches[2] = nb;
+    pass_launches[3] = nrot > 0 ? 1 : 0;
+    return rc;
 }
 
 extern "C" int vesper_topn(const float *scores, int n, int stride, int topn, int32_t *idx_out, void *stream) {

@@ -372,8 +372,10 @@ def target_spectra_device(data, vec, mode, ave, probs=None, dev=None):
     return spec
 
 
-def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, batch=0, dev=None):
-    """vesper_search: (scores f32 [n][nscore], lin int32 [n][nscore]) CUDA tensors."""
+def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, batch=0, dev=None, profile=None):
+    """vesper_search: (scores f32 [n][nscore], lin int32 [n][nscore]) CUDA tensors.
+    With ``profile`` (a dict), vesper_search_profile runs instead and the dict
+    receives the per-pass device milliseconds and launch counts."""
     dev = dev or default_device()
     d = int(data.shape[0])
     code = mode if isinstance(mode, int) else MODE_CODES[mode]
@@ -384,9 +386,17 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
     ws_bytes = _native.size_query("vesper_search_workspace_size", d, code, int(batch), max(n, 1))
     ws = dev.workspace(("search", d, code, int(batch)), ws_bytes)
     mixarr = (ctypes.c_double * 5)(*[float(v) for v in mix]) if mix is not None else None
-    _native.check(dev.lib.vesper_search(_ptr(spec), _ptr(data), _ptr(vec), _ptr(probs), d, code, float(ave or 0.0),
-                                        _ptr(rotmats), n, mixarr, _ptr(scores), _ptr(lin), int(batch), _ptr(ws),
-                                        ws.numel(), dev.stream))
+    args = (_ptr(spec), _ptr(data), _ptr(vec), _ptr(probs), d, code, float(ave or 0.0), _ptr(rotmats), n, mixarr,
+            _ptr(scores), _ptr(lin), int(batch), _ptr(ws), ws.numel(), dev.stream)
+    if profile is None:
+        _native.check(dev.lib.vesper_search(*args))
+    else:
+        ms = (ctypes.c_float * 4)()
+        nl = (ctypes.c_int * 4)()
+        _native.check(dev.lib.vesper_search_profile(*args, ms, nl))
+        for k in range(4):
+            profile.setdefault("pass_ms", [0.0] * 4)[k] += ms[k]
+            profile.setdefault("pass_launches", [0] * 4)[k] += nl[k]
     return scores, lin
 
 
