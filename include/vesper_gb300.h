@@ -166,6 +166,24 @@ int vesper_search_profile(const void *spectra, const double *data, const float *
                           float *scores_out, int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes,
                           void *stream, float *pass_ms, int *pass_launches);
 
+/* vesper_search without a workspace argument.  No counterpart in the
+ * reference: it serves callers that cannot allocate device memory
+ * themselves (for example code running while a global-mode stream capture is
+ * active elsewhere in the process, or a host application that provides only
+ * pre-allocated inputs and outputs under a fixed device-memory budget).  Its
+ * scratch is a fixed 16 MiB array inside this library, reserved on every GPU
+ * that loads the library until the process exits; it allocates nothing.
+ * Same arguments and results as vesper_search with batch = 1.  Rejects, with
+ * VESPER_ERR_UNSUPPORTED, any call whose
+ * vesper_search_workspace_size(dim, mode, 1, nrot) exceeds 16 MiB (mode V
+ * fits up to dim 75 with the 24,624 rotations of a 10-degree grid).  The
+ * first call on each device looks up the array's device address: make it
+ * before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU (other streams or host threads) race: serialise them. */
+int vesper_search_static(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
+                         int mode, double ave, const float *rotmats, int nrot, const double *mix, float *scores_out,
+                         int32_t *lin_out, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Stable top-N: indices of the ``topn`` largest of scores[i*stride]
  * (i < n), ties to the lower index -- Python's stable

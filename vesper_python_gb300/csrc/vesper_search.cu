@@ -9,6 +9,7 @@
 // The three passes of one batch keep S and U resident in L2 (the library
 // default batch keeps them well under the 129 MB L2).
 #include <algorithm>
+#include <mutex>
 
 #include "vesper_common.cuh"
 
@@ -810,6 +811,62 @@ extern "C" int vesper_search_profile(const void *spectra, const double *data, co
     pass_launches[0] = pass_launches[1] = pass_launches[2] = nb;
     pass_launches[3] = nrot > 0 ? 1 : 0;
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Search without caller-provided scratch.
+//
+// For callers that cannot allocate device memory themselves -- for example
+// code that runs while another part of the process holds a stream capture in
+// global mode (cudaMalloc then fails), or a host application that hands this
+// library only pre-allocated input and output buffers under a fixed
+// device-memory budget.  Its scratch is the fixed array below, which the CUDA
+// module reserves on every GPU that loads this library and keeps until the
+// process exits.  All calls on a device share it: calls that overlap on the
+// GPU (two streams, or two host threads) race on it, so serialise them.
+// ---------------------------------------------------------------------------
+namespace vg {
+constexpr size_t kStaticScratchBytes = 16ull << 20;   // 16 MiB
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_static_mu;
+static void *g_static_ptr[kMaxDevices] = {};
+}  // namespace vg
+
+// The host-side name g_static_scratch is only a stand-in for the device array,
+// so its device address is looked up once per device (with that device
+// current) and cached; the first call on each device does this set-up, so make
+// that first call before any stream capture.
+extern "C" int vesper_search_static(const void *spectra, const double *data, const float *vec, const float *probs,
+                                    int dim, int mode, double ave, const float *rotmats, int nrot, const double *mix,
+                                    float *scores_out, int32_t *lin_out, void *stream) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return cuda_check("vesper_search_static: cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return fail(VESPER_ERR_UNSUPPORTED, "vesper_search_static: device %d", dev);
+    void *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_static_mu);
+        if (!g_static_ptr[dev]) {
+            void *p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+            if (e != cudaSuccess || !p)
+                return fail(VESPER_ERR_CUDA, "vesper_search_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            g_static_ptr[dev] = p;
+        }
+        scratch = g_static_ptr[dev];
+    }
+    size_t need = 0;
+    int rc = vesper_search_workspace_size(dim, mode, 1, nrot, &need);
+    if (rc) return rc;
+    if (need > kStaticScratchBytes)
+        return fail(VESPER_ERR_UNSUPPORTED,
+                    "vesper_search_static: dim=%d mode=%d nrot=%d needs %zu bytes of scratch, above its fixed %zu "
+                    "(use vesper_search with a workspace)", dim, mode, nrot, need, (size_t)kStaticScratchBytes);
+    // one rotation per pipeline step; the keys each rotation reads are zeroed by
+    // its own first pass, so nothing left in the array by an earlier call matters
+    return search_impl(spectra, data, vec, probs, dim, mode, ave, rotmats, nrot, mix, scores_out, lin_out, 1, scratch,
+                       kStaticScratchBytes, stream, nullptr);
 }
 
 extern "C" int vesper_topn(const float *scores, int n, int stride, int topn, int32_t *idx_out, void *stream) {
