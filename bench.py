@@ -233,12 +233,12 @@ def run_gb300(args):
     sm_mhz = clocks.get("sm_mhz") or 1900.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "search_traffic.json")
-    if os.path.exists(tr_path):
-        try:
-            traffic = json.load(open(tr_path)).get(names[top])
-        except (OSError, ValueError):
-            traffic = None
+    tr_path = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.txt")
+    if os.path.exists(tr_path) and args.mode == "V":
+        for ln in open(tr_path):
+            f = ln.split()
+            if len(f) == 2 and not ln.startswith("#") and f[0] == names[top]:
+                traffic = int(f[1])
     search_ms = sum(prof["pass_ms"])
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
