@@ -128,9 +128,9 @@ def pass_model(dim, mode):
     G = 2 if mode == "prob" else 1
     axis = 2.5 * N * np.log2(dim)          # one axis of one real 3-D FFT
     return {
-        "query_zy": {"flop": C * 2 * axis, "bytes": N * 20 + C * Nh * 8},
-        "x_corr": {"flop": C * axis + 8 * C * Nh + G * axis, "bytes": C * Nh * 8 * 2 + G * Nh * 8},
-        "inv_argmax": {"flop": G * 2 * axis + N, "bytes": G * Nh * 8},
+        "pass_a": {"flop": C * 2 * axis, "bytes": N * 20 + C * Nh * 8},
+        "pass_b": {"flop": C * axis + 8 * C * Nh + G * axis, "bytes": C * Nh * 8 * 2 + G * Nh * 8},
+        "pass_c": {"flop": G * 2 * axis + N, "bytes": G * Nh * 8},
     }
 
 
@@ -220,7 +220,7 @@ def run_gb300(args):
         return
     # ---- roofline of the dominant kernel -------------------------------------
     pm = pass_model(dim, args.mode if args.mode != "V" else "V")
-    names = ["query_zy", "x_corr", "inv_argmax"]
+    names = ["pass_a", "pass_b", "pass_c"]
     pass_ms = prof["pass_ms"][:3]
     pass_n = prof["pass_launches"][:3]
     top = int(np.argmax(pass_ms))

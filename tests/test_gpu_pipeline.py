@@ -1,0 +1,122 @@
+"""End-to-end GPU path against the reference's recorded output: the float64
+rescoring kernel against the oracle's get_score, the device-resident
+alignment pipeline and the ``main.py orig`` command line on the golden pair
+(128^3 / 64^3 maps at s = 7, A = 30, d = 13)."""
+import contextlib
+import io
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import vesper_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _field(rng, d, zero_frac=0.5):
+    data = rng.uniform(0.1, 2.0, size=(d, d, d))
+    data[rng.random((d, d, d)) < zero_frac] = 0.0
+    vec = rng.normal(size=(d, d, d, 3)).astype(np.float32)
+    vec[data == 0] = 0
+    return data, vec
+
+
+@pytest.mark.parametrize("trans", [(0, 0, 0), (3, 12, 7), (12, 1, 6), (6, 7, 0)])
+def test_rescore_matches_oracle_get_score(dev, trans):
+    from vesper_python_gb300 import vesper as vg
+    rng = np.random.default_rng(sum(trans) + 3)
+    d = 13
+    tdata, tvec = _field(rng, d)
+    sdata, svec = _field(rng, d)
+    pos = tdata[tdata > 0]
+    tave, tstd, tpstd = np.mean(pos), np.linalg.norm(pos), np.linalg.norm(pos - np.mean(pos))
+    ov, nm, total, cc, pcc, score, sco = orc.get_score(tdata, tvec, tave, tstd, tpstd, sdata, svec, trans)
+
+    class T:
+        pass
+
+    t = T()
+    t.data, t.vec, t.ave, t.std, t.std_norm_ave = tdata, tvec, tave, tstd, tpstd
+    sr = vg.get_score_device(t, dev.to_dev(sdata), dev.to_dev(svec), trans, dev=dev)
+    assert (sr.nm, sr.total) == (nm, total)
+    assert abs(sr.cc - cc) <= 1e-12 * max(1.0, abs(cc))
+    assert abs(sr.pcc - pcc) <= 1e-12 * max(1.0, abs(pcc))
+    # the reference's per-voxel dot products are float32; ours are float64
+    assert abs(sr.score - score) <= 1e-5 * max(1.0, abs(score))
+    assert np.allclose(sr.sco_arr, sco, rtol=1e-5, atol=1e-5)
+
+
+def _model_lines(text, prefix):
+    return [ln for ln in text.splitlines() if re.match(rf"^{re.escape(prefix)}\d+ Rotation=", ln)]
+
+
+def test_aligner_matches_golden_refined_models(dev, golden_dir):
+    from vesper_python_gb300 import align, synth
+    g = np.load(os.path.join(golden_dir, "search_pair128.npz"))
+    pair = synth.workload_pair("pair128_s7_a30", seed=0)
+    al = align.Aligner(dev)
+    p = align.AlignParams(t=0.1, T=0.1, g=16.0, s=7.0, A=30.0, N=10, mode="VecProduct")
+    res = al.align_device(dev.to_dev(pair.map1), dev.to_dev(pair.map2), 1.0, 1.0, pair.orig1, pair.orig2, p)
+    assert res.dim == int(g["dim"])
+    ang = np.array([m.angle for m in res.models])
+    tr = np.array([m.vec_trans for m in res.models])
+    assert np.array_equal(ang, g["V_refined_angle"])
+    assert np.array_equal(tr, g["V_refined_trans"])
+    assert np.allclose([m.vec_score for m in res.models], g["V_refined_score"], rtol=1e-4)
+
+
+def test_main_orig_cli_matches_reference_stdout(dev, golden_dir, tmp_path):
+    """Rotation/translation lines byte-identical to the reference's stdout;
+    the printed scores within 1e-4 relative."""
+    from vesper_python_gb300 import main as cli
+    from vesper_python_gb300 import mrc, synth
+    pair = synth.workload_pair("pair128_s7_a30", seed=0)
+    a = tmp_path / "map1.mrc"
+    b = tmp_path / "map2.mrc"
+    mrc.write_mrc(a, np.swapaxes(pair.map1, 0, 2), 1.0, pair.orig1)
+    mrc.write_mrc(b, np.swapaxes(pair.map2, 0, 2), 1.0, pair.orig2)
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        cli.main(["orig", "-a", str(a), "-b", str(b), "-t", "0.1", "-T", "0.1", "-s", "7", "-A", "30"])
+    out = buf.getvalue()
+    ref = open(os.path.join(golden_dir, "search_pair128_V.txt")).read()
+    setup = open(os.path.join(golden_dir, "search_pair128_setup.txt")).read()
+    for prefix in ("M", "#"):
+        assert _model_lines(out, prefix) == _model_lines(ref, prefix)
+    for key in ("#dmax=", "Nvox=", "cent=", "ori="):
+        assert [ln for ln in out.splitlines() if ln.startswith(key)] == \
+            [ln for ln in setup.splitlines() if ln.startswith(key)]
+
+    def nums(text, key):
+        return [float(re.search(rf"{key}\s*([-0-9.e+]+)", ln).group(1)) for ln in text.splitlines() if key in ln]
+
+    for key in ("Score=", "CC=", "PCC=", "Overlap="):
+        o, r = nums(out, key), nums(ref, key)
+        assert len(o) == len(r) == 10
+        assert np.allclose(o, r, rtol=1e-4, atol=1e-6), key
+    sums_o, sums_r = nums(out, "SUM="), nums(setup, "SUM=")
+    assert np.allclose(sums_o, sums_r, rtol=1e-12)
+
+
+def test_prob_pipeline_top_models(dev, golden_dir, tmp_path):
+    """main.py prob on the golden prob pair: the refined models' rotations and
+    translations match the reference's stdout."""
+    from vesper_python_gb300 import main as cli
+    from vesper_python_gb300 import mrc, synth
+    pair = synth.make_pair(0, 128, 400, 40.0, with_prob=True, threshold=0.1)
+    a, b = tmp_path / "m1.mrc", tmp_path / "m2.mrc"
+    mrc.write_mrc(a, np.swapaxes(pair.map1, 0, 2), 1.0, pair.orig1)
+    mrc.write_mrc(b, np.swapaxes(pair.map2, 0, 2), 1.0, pair.orig2)
+    pa, pb = tmp_path / "p1.npy", tmp_path / "p2.npy"
+    # main.py swaps the .npy axes like the MRC data: store them in file order
+    np.save(pa, np.swapaxes(pair.prob1, 0, 2))
+    np.save(pb, np.swapaxes(pair.prob2, 0, 2))
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        cli.main(["prob", "-a", str(a), "-npa", str(pa), "-b", str(b), "-npb", str(pb), "-t", "0.1", "-T", "0.1",
+                  "-s", "7", "-A", "30", "-alpha", "0.5"])
+    out = buf.getvalue()
+    ref = open(os.path.join(golden_dir, "prob_pair128.txt")).read()
+    assert _model_lines(out, "#") == _model_lines(ref, "#")

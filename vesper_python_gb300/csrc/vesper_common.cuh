@@ -125,4 +125,71 @@ __device__ __forceinline__ void rotate_vec(const float *F, float v0, float v1, f
     }
 }
 
+// ---- search-wide definitions ------------------------------------------------------
+constexpr int kThreads = 256;
+constexpr int kRY = 8;          // rows per z-chunk of the float64 target pass (even: rows pair up)
+constexpr int kPairs = kRY / 2;
+
+struct Query {
+    const double *data;
+    const float *vec;
+    const float *probs;
+    int d;
+    double ave;
+};
+
+// prob-mode z-score mixing constants (float32, as numpy 1.21 computes them)
+struct Mix {
+    float one_minus_alpha, alpha, vave, vstd, pave, pstd;
+};
+
+__host__ __device__ inline int mode_nch(int mode) {
+    return mode == VESPER_MODE_VEC ? 3 : (mode == VESPER_MODE_PROB ? 7 : 1);
+}
+__host__ __device__ inline int mode_ngrp(int mode) { return mode == VESPER_MODE_PROB ? 2 : 1; }
+
+// After a forward FFT of line Z = a + i b, the half spectra of a and b.
+template <typename C>
+__device__ __forceinline__ void unpack_pair(C Zk, C Zn, C &A, C &B) {
+    using R = typename Real<C>::T;
+    const R h = (R)0.5;
+    A = mk(h * (Zk.x + Zn.x), h * (Zk.y - Zn.y));
+    B = mk(h * (Zk.y + Zn.y), -h * (Zk.x - Zn.x));
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+__host__ __device__ inline size_t smem_target_a(int d, int H) {
+    return (size_t)d * sizeof(double2) + (size_t)d * H * sizeof(double2) + (size_t)kPairs * d * sizeof(double2) +
+           ((d * sizeof(short) + 15) & ~15);
+}
+__host__ __device__ inline size_t smem_target_b(int d, int W) {
+    return (size_t)d * sizeof(double2) + (size_t)d * W * sizeof(double2) + ((d * sizeof(short) + 15) & ~15);
+}
+
+// Opt-in shared memory per block of the current device (host).
+inline int smem_limit() {
+    static int lim = 0;
+    if (!lim) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0)
+            v = 227 * 1024;
+        lim = v;
+    }
+    return lim;
+}
+
+template <typename K>
+inline void allow_smem(K kernel, size_t bytes) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 }  // namespace vg

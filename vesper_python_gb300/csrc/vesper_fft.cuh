@@ -23,6 +23,8 @@ struct FftPlan {
     int n;
     int nst;
     int rad[kMaxStages];   // radix of stage s, stage 0 innermost
+    int st0[kMaxStages];   // start of stage s in the butterfly tables (sum of n / rad over earlier stages)
+    int ntab;              // total butterfly-table entries
 };
 
 // ---- complex helpers (float2 / double2) -----------------------------------
@@ -286,5 +288,108 @@ __device__ void fft_run(C *buf, const Lines &g, const FftPlan &P, const C *tw, b
         L = Ln;
     }
 }
+
+// ---------------------------------------------------------------------------
+// Division-free line FFTs.  Per CTA, stage tables give for butterfly bf of
+// stage s its element offset inside the line (blk * L * p + j) and the offset
+// of its twiddles in tw[]; each thread owns one line (two when there are more
+// lines than threads) and a fixed stride through that line's butterflies, so
+// the inner loops carry no integer division.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void fft_stage_tables(const FftPlan &P, short *off, short *two) {
+    int L = 1;
+    for (int s = 0; s < P.nst; ++s) {
+        const int p = P.rad[s], nbf = P.n / p;
+        for (int bf = threadIdx.x; bf < nbf; bf += blockDim.x) {
+            const int j = bf % L, blk = bf / L;
+            off[P.st0[s] + bf] = (short)(blk * L * p + j);
+            two[P.st0[s] + bf] = (short)((L - 1) + j * (p - 1));
+        }
+        L *= p;
+    }
+}
+
+struct LineSlot {
+    int base0, base1;   // element offsets of the thread's lines
+    int sub0, nsub;     // first butterfly and butterfly stride inside line 0
+    bool a0, a1;
+};
+
+// Line l starts at (l / nin) * so + (l % nin) * si.  Supports count <= 2 * blockDim.
+__device__ __forceinline__ LineSlot line_slot(int count, int nin, int so, int si) {
+    LineSlot s;
+    const int T = blockDim.x, t = threadIdx.x;
+    if (count >= T) {
+        s.nsub = 1;
+        s.sub0 = 0;
+        s.a0 = true;
+        s.base0 = (t / nin) * so + (t % nin) * si;
+        const int l1 = t + T;
+        s.a1 = l1 < count;
+        s.base1 = s.a1 ? (l1 / nin) * so + (l1 % nin) * si : 0;
+    } else {
+        s.nsub = T / count;
+        const int l = t % count;
+        s.sub0 = t / count;
+        s.a0 = s.sub0 < s.nsub;
+        s.a1 = false;
+        s.base0 = (l / nin) * so + (l % nin) * si;
+        s.base1 = 0;
+    }
+    return s;
+}
+
+template <int P, bool INV, typename C>
+__device__ __forceinline__ void stage_loop(C *buf, const LineSlot &ls, int es, int esL, int nbf, const short *off,
+                                           const short *two, const C *tw) {
+    if (ls.a0)
+        for (int bf = ls.sub0; bf < nbf; bf += ls.nsub) butterfly<P, INV>(buf + ls.base0 + off[bf] * es, esL, tw + two[bf]);
+    if (ls.a1)
+        for (int bf = 0; bf < nbf; ++bf) butterfly<P, INV>(buf + ls.base1 + off[bf] * es, esL, tw + two[bf]);
+}
+
+template <bool INV, typename C>
+__device__ void fft_lines(C *buf, const LineSlot &ls, int es, const FftPlan &P, const short *off, const short *two,
+                          const C *tw) {
+    int L = 1;
+    for (int s = 0; s < P.nst; ++s) {
+        const int p = P.rad[s];
+        const int nbf = P.n / p, esL = L * es;
+        const short *o = off + P.st0[s], *w = two + P.st0[s];
+        switch (p) {
+            case 2: stage_loop<2, INV>(buf, ls, es, esL, nbf, o, w, tw); break;
+            case 3: stage_loop<3, INV>(buf, ls, es, esL, nbf, o, w, tw); break;
+            case 4: stage_loop<4, INV>(buf, ls, es, esL, nbf, o, w, tw); break;
+            case 5: stage_loop<5, INV>(buf, ls, es, esL, nbf, o, w, tw); break;
+            case 7: stage_loop<7, INV>(buf, ls, es, esL, nbf, o, w, tw); break;
+            case 11: stage_loop<11, INV>(buf, ls, es, esL, nbf, o, w, tw); break;
+            case 13: stage_loop<13, INV>(buf, ls, es, esL, nbf, o, w, tw); break;
+            default: break;
+        }
+        __syncthreads();
+        L *= p;
+    }
+}
+
+// Walk a flattened 2-D index space (rows of ``inner`` items) in steps of
+// blockDim.x without division: (o, i) advances by (T / inner, T % inner).
+struct Walk2 {
+    int o, i, so, si, inner;
+    __device__ __forceinline__ Walk2(int inner_) : inner(inner_) {
+        const int T = blockDim.x, t = threadIdx.x;
+        o = t / inner_;
+        i = t % inner_;
+        so = T / inner_;
+        si = T % inner_;
+    }
+    __device__ __forceinline__ void next() {
+        o += so;
+        i += si;
+        if (i >= inner) {
+            i -= inner;
+            ++o;
+        }
+    }
+};
 
 }  // namespace vg

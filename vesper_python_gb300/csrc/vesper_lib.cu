@@ -49,8 +49,14 @@ bool make_plan(int n, FftPlan *plan) {
     if (m != 1 || big > 1 || k > kMaxStages) return false;
     plan->n = n;
     plan->nst = k;
-    for (int i = 0; i < k; ++i) plan->rad[i] = rad[i];
-    if (n == 1) { plan->nst = 0; }
+    int acc = 0;
+    for (int i = 0; i < k; ++i) {
+        plan->rad[i] = rad[i];
+        plan->st0[i] = acc;
+        acc += n / rad[i];
+    }
+    plan->ntab = acc;
+    if (n == 1) { plan->nst = 0; plan->ntab = 0; }
     return true;
 }
 

@@ -1,0 +1,408 @@
+// The three per-batch passes of the rotational search (included by
+// vesper_search.cu).
+//
+//   pack   (once per call)  query fields -> float4 source: (vx, vy, vz, mask) for
+//                           V / prob, (mode value, 0, 0, mask) for O/C/P/L, plus
+//                           float4 probabilities for prob; mask = data != 0
+//   A  k_pass_a   grid (d, nb)       rotate one x plane of C channels, z R2C
+//                                    (two real rows per complex line), y FFT -> S
+//   B  k_pass_b   grid (Nh/W, nb)    x FFT, * conj target, sum per group,
+//                                    inverse x FFT -> U
+//   C  k_pass_c   grid (d, nb)       inverse y, inverse z (C2R, row pairs),
+//                                    scores, first-index argmax -> keys
+//
+// Every FFT runs over all lines of a plane at once with the division-free
+// stage tables of vesper_fft.cuh; row strides are padded to odd element
+// counts so that lines handled by neighbouring threads fall in distinct
+// shared-memory banks.
+#pragma once
+
+#include "vesper_common.cuh"
+
+namespace vg {
+
+struct Src {
+    const float4 *q4;     // [N]
+    const float4 *p4;     // [N] or null
+    const double *data;   // [N] (Laplacian needs the float64 density)
+    int d;
+};
+
+__host__ __device__ inline int odd_up(int n) { return n | 1; }
+
+// ---- pack -------------------------------------------------------------------
+template <int MODE>
+__global__ void k_pack(const double *data, const float *vec, const float *probs, int d, double ave, float4 *q4,
+                       float4 *p4) {
+    const size_t n = (size_t)d * d * d;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double v = data[i];
+        const float m = v != 0.0 ? 1.f : 0.f;
+        float4 o;
+        if (MODE == VESPER_MODE_VEC || MODE == VESPER_MODE_PROB) {
+            o = make_float4(vec[3 * i], vec[3 * i + 1], vec[3 * i + 2], m);
+        } else {
+            float val = 0.f;   // query transforms, VESPER_1_prob_new.py:548-553
+            if (MODE == VESPER_MODE_OVERLAP) val = v > 0 ? 1.f : 0.f;
+            if (MODE == VESPER_MODE_CC) val = v > 0 ? (float)v : 0.f;
+            if (MODE == VESPER_MODE_PCC) val = v > 0 ? (float)__dsub_rn(v, ave) : 0.f;
+            o = make_float4(val, 0.f, 0.f, m);
+        }
+        q4[i] = o;
+        if (MODE == VESPER_MODE_PROB) p4[i] = make_float4(probs[i], probs[n + i], probs[2 * n + i], probs[3 * n + i]);
+    }
+}
+
+// ---- gather -----------------------------------------------------------------
+// Winning source (last reference row passing bounds and mask) of destination
+// (x, y, z): its index, or -1.  Same rule as gather_src, reading the packed
+// source once per candidate.
+__device__ __forceinline__ int gather4(const float *F, int d, int x, int y, int z, const float4 *q4, float4 &out) {
+    int cx[2], cy[2], cz[2];
+    const int nx = gather_cands(x, d, cx), ny = gather_cands(y, d, cy), nz = gather_cands(z, d, cz);
+    const float hc = 0.5f * (float)d;
+    for (int a = 0; a < nz; ++a)
+        for (int b = 0; b < nx; ++b)
+            for (int e = 0; e < ny; ++e) {
+                int ox, oy, oz;
+                if (!old_index(F, d, hc, (float)cx[b] - hc, (float)cy[e] - hc, (float)cz[a] - hc, ox, oy, oz))
+                    continue;
+                const int i = (ox * d + oy) * d + oz;
+                const float4 v = q4[i];
+                if (v.w != 0.f) {
+                    out = v;
+                    return i;
+                }
+            }
+    return -1;
+}
+
+// Probability channels, each with its own mask p != 0 (VESPER_1_prob_new.py:1245-1297).
+__device__ __forceinline__ float4 gather_probs(const float *F, int d, int x, int y, int z, const float4 *p4) {
+    int cx[2], cy[2], cz[2];
+    const int nx = gather_cands(x, d, cx), ny = gather_cands(y, d, cy), nz = gather_cands(z, d, cz);
+    const float hc = 0.5f * (float)d;
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool s0 = false, s1 = false, s2 = false, s3 = false;
+    for (int a = 0; a < nz; ++a)
+        for (int b = 0; b < nx; ++b)
+            for (int e = 0; e < ny; ++e) {
+                int ox, oy, oz;
+                if (!old_index(F, d, hc, (float)cx[b] - hc, (float)cy[e] - hc, (float)cz[a] - hc, ox, oy, oz))
+                    continue;
+                const float4 v = p4[(ox * d + oy) * d + oz];
+                if (!s0 && v.x != 0.f) { o.x = v.x; s0 = true; }
+                if (!s1 && v.y != 0.f) { o.y = v.y; s1 = true; }
+                if (!s2 && v.z != 0.f) { o.z = v.z; s2 = true; }
+                if (!s3 && v.w != 0.f) { o.w = v.w; s3 = true; }
+                if (s0 && s1 && s2 && s3) return o;
+            }
+    return o;
+}
+
+// Channel values of the rotated query at (x, y, z): out[c] for every channel.
+template <int MODE>
+__device__ __forceinline__ void sample(const Src &s, const float *F, int x, int y, int z, float *out) {
+    const int d = s.d;
+    float4 v;
+    if (MODE == VESPER_MODE_LAPLACIAN) {
+        // laplacian_filter of the rotated density (VESPER_1_prob_new.py:494-526), float64
+        auto D = [&](int xx, int yy, int zz) -> double {
+            float4 w;
+            const int i = gather4(F, d, xx, yy, zz, s.q4, w);
+            return i >= 0 ? s.data[i] : 0.0;
+        };
+        const double c = D(x, y, z);
+        double acc = 0.0;
+        if (c > 0) {
+            acc = __dmul_rn(-6.0, c);
+            if (x + 1 < d) acc = __dadd_rn(acc, D(x + 1, y, z));
+            if (x - 1 >= 0) acc = __dadd_rn(acc, D(x - 1, y, z));
+            if (y + 1 < d) acc = __dadd_rn(acc, D(x, y + 1, z));
+            if (y - 1 >= 0) acc = __dadd_rn(acc, D(x, y - 1, z));
+            if (z + 1 < d) acc = __dadd_rn(acc, D(x, y, z + 1));
+            if (z - 1 >= 0) acc = __dadd_rn(acc, D(x, y, z - 1));
+        }
+        out[0] = (float)acc;
+        return;
+    }
+    const bool hit = gather4(F, d, x, y, z, s.q4, v) >= 0;
+    if (MODE == VESPER_MODE_VEC || MODE == VESPER_MODE_PROB) {
+        float r[3] = {0.f, 0.f, 0.f};
+        if (hit) rotate_vec(F, v.x, v.y, v.z, r);
+        out[0] = r[0];
+        out[1] = r[1];
+        out[2] = r[2];
+        if (MODE == VESPER_MODE_PROB) {
+            const float4 p = gather_probs(F, d, x, y, z, s.p4);
+            out[3] = p.x;
+            out[4] = p.y;
+            out[5] = p.z;
+            out[6] = p.w;
+        }
+    } else {
+        out[0] = hit ? v.x : 0.f;
+    }
+}
+
+// ---- shared-memory layout helpers ---------------------------------------------
+struct PlaneGeom {
+    int d, H, npairs, Zp, Hp;   // npairs = (d+1)/2 packed z lines; padded strides
+};
+__host__ __device__ inline PlaneGeom plane_geom(int d) {
+    PlaneGeom g;
+    g.d = d;
+    g.H = d / 2 + 1;
+    g.npairs = (d + 1) / 2;
+    g.Zp = odd_up(d);
+    g.Hp = odd_up(g.H);
+    return g;
+}
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+// common head: tw (float2 d) | rev (short d) | off, two (short ntab each)
+__host__ __device__ inline size_t smem_head(int d, int ntab) {
+    return align16((size_t)d * sizeof(float2)) + align16((size_t)d * sizeof(short)) +
+           2 * align16((size_t)ntab * sizeof(short));
+}
+struct Head {
+    float2 *tw;
+    short *rev, *off, *two;
+    unsigned char *rest;
+};
+__device__ __forceinline__ Head carve_head(unsigned char *smem, int d, int ntab) {
+    Head h;
+    h.tw = (float2 *)smem;
+    h.rev = (short *)(smem + align16((size_t)d * sizeof(float2)));
+    h.off = (short *)((unsigned char *)h.rev + align16((size_t)d * sizeof(short)));
+    h.two = (short *)((unsigned char *)h.off + align16((size_t)ntab * sizeof(short)));
+    h.rest = (unsigned char *)h.two + align16((size_t)ntab * sizeof(short));
+    return h;
+}
+__device__ __forceinline__ void init_head(const FftPlan &P, const Head &h) {
+    fft_tables(P, h.rev, h.tw);
+    fft_stage_tables(P, h.off, h.two);
+}
+
+// ---- pass A -------------------------------------------------------------------
+struct PassA2 {
+    Src src;
+    const float *rotmats;
+    int r0, nch, cchunk, nscore;
+    FftPlan P;
+    float2 *S;                    // [batch][nch][d][d][H]
+    unsigned long long *keys;     // [nrot][nscore]
+};
+
+__host__ __device__ inline size_t smem_a2(int d, int ntab, int cchunk) {
+    const PlaneGeom g = plane_geom(d);
+    return smem_head(d, ntab) + align16(16 * sizeof(float)) +
+           (size_t)cchunk * ((size_t)g.npairs * g.Zp + (size_t)d * g.Hp) * sizeof(float2);
+}
+
+template <int MODE, int NCH>
+__global__ void __launch_bounds__(512) k_pass_a(const PassA2 a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const PlaneGeom g = plane_geom(a.src.d);
+    const int d = g.d, H = g.H, np = g.npairs, Zp = g.Zp, Hp = g.Hp;
+    const int x = blockIdx.x, b = blockIdx.y, r = a.r0 + b;
+    const Head h = carve_head(smem, d, a.P.ntab);
+    float *F = (float *)h.rest;
+    float2 *zbuf = (float2 *)(h.rest + align16(16 * sizeof(float)));
+    float2 *plane = zbuf + (size_t)a.cchunk * np * Zp;
+    init_head(a.P, h);
+    if (threadIdx.x < 9) F[threadIdx.x] = a.rotmats[(size_t)r * 9 + threadIdx.x];
+    if (x == 0 && threadIdx.x < a.nscore) a.keys[(size_t)r * a.nscore + threadIdx.x] = 0ull;
+    __syncthreads();
+    for (int c0 = 0; c0 < NCH; c0 += a.cchunk) {
+        const int cn = min(a.cchunk, NCH - c0);
+        // gather two rows (2p, 2p+1) per item into packed z lines, digit-reversed z
+        for (Walk2 w(d); w.o < np; w.next()) {
+            const int p = w.o, z = w.i, y0 = 2 * p;
+            float v0[NCH], v1[NCH];
+            sample<MODE>(a.src, F, x, y0, z, v0);
+            if (y0 + 1 < d) {
+                sample<MODE>(a.src, F, x, y0 + 1, z, v1);
+            } else {
+#pragma unroll
+                for (int c = 0; c < NCH; ++c) v1[c] = 0.f;
+            }
+            const int rz = h.rev[z];
+#pragma unroll
+            for (int c = 0; c < NCH; ++c)
+                if (c >= c0 && c < c0 + cn) zbuf[((c - c0) * np + p) * Zp + rz] = make_float2(v0[c], v1[c]);
+        }
+        __syncthreads();
+        fft_lines<false>(zbuf, line_slot(cn * np, cn * np, 0, Zp), 1, a.P, h.off, h.two, h.tw);
+        // unpack the two half spectra into rows rev(y) of the plane
+        for (int c = 0; c < cn; ++c) {
+            const float2 *zl = zbuf + (size_t)c * np * Zp;
+            float2 *pl = plane + (size_t)c * d * Hp;
+            for (Walk2 w(H); w.o < np; w.next()) {
+                const int p = w.o, k = w.i, y = 2 * p;
+                float2 A, B;
+                unpack_pair(zl[p * Zp + k], zl[p * Zp + (k == 0 ? 0 : d - k)], A, B);
+                pl[h.rev[y] * Hp + k] = A;
+                if (y + 1 < d) pl[h.rev[y + 1] * Hp + k] = B;
+            }
+        }
+        __syncthreads();
+        fft_lines<false>(plane, line_slot(cn * H, H, d * Hp, 1), Hp, a.P, h.off, h.two, h.tw);
+        for (int c = 0; c < cn; ++c) {
+            float2 *dst = a.S + (((size_t)b * NCH + c0 + c) * d + x) * (size_t)d * H;
+            const float2 *pl = plane + (size_t)c * d * Hp;
+            for (Walk2 w(H); w.o < d; w.next()) dst[w.o * H + w.i] = pl[w.o * Hp + w.i];
+        }
+        __syncthreads();
+    }
+}
+
+// ---- pass B -------------------------------------------------------------------
+struct PassB2 {
+    const float2 *S;
+    const float2 *T;     // [nch][d][d][H] conj target spectrum
+    float2 *U;           // [batch][ngrp][d][d][H]
+    int d, nch, ngrp, split, W;
+    FftPlan P;
+};
+
+__host__ __device__ inline size_t smem_b2(int d, int ntab, int nch, int ngrp, int W) {
+    return smem_head(d, ntab) + (size_t)(nch + ngrp) * d * W * sizeof(float2);
+}
+
+__global__ void __launch_bounds__(512) k_pass_b(const PassB2 a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int d = a.d, H = d / 2 + 1, dH = d * H, W = a.W;
+    const int j0 = blockIdx.x * W, b = blockIdx.y;
+    const Head h = carve_head(smem, d, a.P.ntab);
+    float2 *buf = (float2 *)h.rest;
+    float2 *pbuf = buf + (size_t)a.nch * d * W;
+    init_head(a.P, h);
+    __syncthreads();
+    const float2 *src = a.S + (size_t)b * a.nch * d * dH;
+    for (int c = 0; c < a.nch; ++c)
+        for (Walk2 w(W); w.o < d; w.next()) {
+            const int x = w.o, j = j0 + w.i;
+            buf[((size_t)c * d + h.rev[x]) * W + w.i] =
+                j < dH ? src[((size_t)c * d + x) * dH + j] : make_float2(0.f, 0.f);
+        }
+    __syncthreads();
+    fft_lines<false>(buf, line_slot(a.nch * W, W, d * W, 1), W, a.P, h.off, h.two, h.tw);
+    for (int g = 0; g < a.ngrp; ++g) {
+        const int cb = g == 0 ? 0 : a.split, ce = g == 0 ? a.split : a.nch;
+        for (Walk2 w(W); w.o < d; w.next()) {
+            const int x = w.o, j = j0 + w.i;
+            float2 acc = make_float2(0.f, 0.f);
+            if (j < dH)
+                for (int c = cb; c < ce; ++c)
+                    acc = cadd(acc, cmul(a.T[((size_t)c * d + x) * dH + j], buf[((size_t)c * d + x) * W + w.i]));
+            pbuf[((size_t)g * d + h.rev[x]) * W + w.i] = acc;
+        }
+    }
+    __syncthreads();
+    fft_lines<true>(pbuf, line_slot(a.ngrp * W, W, d * W, 1), W, a.P, h.off, h.two, h.tw);
+    float2 *dst = a.U + (size_t)b * a.ngrp * d * dH;
+    for (int g = 0; g < a.ngrp; ++g)
+        for (Walk2 w(W); w.o < d; w.next()) {
+            const int j = j0 + w.i;
+            if (j < dH) dst[((size_t)g * d + w.o) * dH + j] = pbuf[((size_t)g * d + w.o) * W + w.i];
+        }
+}
+
+// ---- pass C -------------------------------------------------------------------
+struct PassC2 {
+    const float2 *U;
+    int d, ngrp, r0, nscore;
+    FftPlan P;
+    Mix mix;
+    unsigned long long *keys;
+};
+
+__host__ __device__ inline size_t smem_c2(int d, int ntab, int ngrp) {
+    const PlaneGeom g = plane_geom(d);
+    return smem_head(d, ntab) + (size_t)ngrp * ((size_t)d * g.Hp + (size_t)g.npairs * g.Zp) * sizeof(float2) +
+           3 * 32 * sizeof(unsigned long long);
+}
+
+template <int SC>
+__global__ void __launch_bounds__(512) k_pass_c(const PassC2 a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const PlaneGeom g = plane_geom(a.d);
+    const int d = g.d, H = g.H, np = g.npairs, Zp = g.Zp, Hp = g.Hp, ngrp = a.ngrp;
+    const int x = blockIdx.x, b = blockIdx.y, r = a.r0 + b;
+    const Head h = carve_head(smem, d, a.P.ntab);
+    float2 *plane = (float2 *)h.rest;
+    float2 *zbuf = plane + (size_t)ngrp * d * Hp;
+    unsigned long long *red = (unsigned long long *)(zbuf + (size_t)ngrp * np * Zp);
+    init_head(a.P, h);
+    __syncthreads();
+    for (int gi = 0; gi < ngrp; ++gi) {
+        const float2 *src = a.U + (((size_t)b * ngrp + gi) * d + x) * (size_t)d * H;
+        float2 *pl = plane + (size_t)gi * d * Hp;
+        for (Walk2 w(H); w.o < d; w.next()) pl[h.rev[w.o] * Hp + w.i] = src[w.o * H + w.i];
+    }
+    __syncthreads();
+    fft_lines<true>(plane, line_slot(ngrp * H, H, d * Hp, 1), Hp, a.P, h.off, h.two, h.tw);
+    // pack row pairs (2p, 2p+1) into full-length lines: Z = A + iB, Hermitian
+    // completion, DC / Nyquist imaginary parts dropped (C2R semantics)
+    for (int gi = 0; gi < ngrp; ++gi) {
+        const float2 *pl = plane + (size_t)gi * d * Hp;
+        float2 *zl = zbuf + (size_t)gi * np * Zp;
+        for (Walk2 w(d); w.o < np; w.next()) {
+            const int p = w.o, k = w.i, y = 2 * p;
+            const bool hb = y + 1 < d;
+            float2 Z;
+            if (k < H) {
+                float2 A = pl[y * Hp + k], B = hb ? pl[(y + 1) * Hp + k] : make_float2(0.f, 0.f);
+                if (k == 0 || 2 * k == d) { A.y = 0.f; B.y = 0.f; }
+                Z = make_float2(A.x - B.y, A.y + B.x);
+            } else {
+                const int kk = d - k;
+                const float2 A = pl[y * Hp + kk], B = hb ? pl[(y + 1) * Hp + kk] : make_float2(0.f, 0.f);
+                Z = make_float2(A.x + B.y, B.x - A.y);
+            }
+            zl[p * Zp + h.rev[k]] = Z;
+        }
+    }
+    __syncthreads();
+    fft_lines<true>(zbuf, line_slot(ngrp * np, ngrp * np, 0, Zp), 1, a.P, h.off, h.two, h.tw);
+    unsigned long long best[3] = {0ull, 0ull, 0ull};
+    for (Walk2 w(d); w.o < np; w.next()) {
+        const int p = w.o, z = w.i;
+        const float2 z0 = zbuf[p * Zp + z];
+        float2 z1 = make_float2(0.f, 0.f);
+        if (SC >= 2) z1 = zbuf[(np + p) * Zp + z];
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int y = 2 * p + half;
+            if (y >= d) break;
+            const uint32_t lin = (uint32_t)((x * d + y) * d + z);
+            const float v0 = half ? z0.y : z0.x;
+            best[0] = max(best[0], make_key(v0, lin));
+            if (SC >= 2) {
+                const float v1 = half ? z1.y : z1.x;
+                best[1] = max(best[1], make_key(v1, lin));
+                if (SC == 3) {
+                    // find_best_trans_mixed (VESPER_1_prob_new.py:1534-1539), float32
+                    const float sv = __fdiv_rn(__fsub_rn(v0, a.mix.vave), a.mix.vstd);
+                    const float sp = __fdiv_rn(__fsub_rn(v1, a.mix.pave), a.mix.pstd);
+                    const float m = __fadd_rn(__fmul_rn(a.mix.one_minus_alpha, sv), __fmul_rn(a.mix.alpha, sp));
+                    best[2] = max(best[2], make_key(m, lin));
+                }
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int s = 0; s < SC; ++s) {
+        const unsigned long long v = warp_max_u64(best[s]);
+        if (lane == 0) red[s * 32 + warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < SC) {
+        unsigned long long v = 0ull;
+        for (int w2 = 0; w2 < nw; ++w2) v = max(v, red[threadIdx.x * 32 + w2]);
+        atomicMax(&a.keys[(size_t)r * a.nscore + threadIdx.x], v);
+    }
+}
+
+}  // namespace vg
