@@ -253,7 +253,8 @@ def run_gb300(args):
                 "h2d_bytes_per_step": int(h1.numel() * 4 + h2.numel() * 4),
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": f"k_{names[top]}", "achieved": round(ach_bytes, 1),
+        "roofline": {"bound": "hbm", "kernel": f"search {names[top]} (k_r{names[top]} register path)",
+                     "achieved": round(ach_bytes, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(ach_bytes / peak, 4), "traffic": traffic,
                      "peak_source": peak_kind,
                      "fp32": {"achieved_tflops": round(ach_flop, 3), "peak_tflops": round(fp32_peak, 1),

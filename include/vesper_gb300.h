@@ -154,17 +154,28 @@ int vesper_search(const void *spectra, const double *data, const float *vec, con
                   float *scores_out, int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes,
                   void *stream);
 
+/* vesper_search with explicit kernel choices, for the autotuner: HOST
+ * opts[3] = {path (-1 automatic, 0 radix-stage passes, 1 register two-step
+ * passes where compiled for this side and mode), channels per pass-A block
+ * (0 automatic), columns per pass-B block (0 automatic)}.  Every choice gives
+ * the same results up to float32 rounding of the FFT. */
+int vesper_search_tuned(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
+                        int mode, double ave, const float *rotmats, int nrot, const double *mix, float *scores_out,
+                        int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes, void *stream,
+                        const int *opts);
+
 /* Profiling form of vesper_search, for benchmarks: the same work, plus CUDA
  * events around every launch.  pass_ms HOST float[4] receives the summed
  * device time of the rotate+z+y passes, the x/correlation passes, the
  * inverse y+z/argmax passes and the final decode; pass_launches HOST int[4]
  * the number of launches of each.  Waits on events up to 16 batches behind
  * the launch front and at the end, so it returns with the stream drained.
- * Not re-entrant: one profiling call at a time per process. */
+ * Not re-entrant: one profiling call at a time per process.  opts as for
+ * vesper_search_tuned (NULL: automatic). */
 int vesper_search_profile(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
                           int mode, double ave, const float *rotmats, int nrot, const double *mix,
                           float *scores_out, int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes,
-                          void *stream, float *pass_ms, int *pass_launches);
+                          void *stream, float *pass_ms, int *pass_launches, const int *opts);
 
 /* vesper_search without a workspace argument.  No counterpart in the
  * reference: it serves callers that cannot allocate device memory
@@ -206,6 +217,41 @@ int vesper_rescore_workspace_size(int dim, size_t *bytes);
 int vesper_rescore(const double *tdata, const float *tvec, double tave, double tstd, double tstd_norm_ave,
                    const double *sdata, const float *svec, int dim, const int32_t *trans, double *result_out,
                    double *sco_out, void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Learned rotation proposal (no counterpart in the reference): a 3-D
+ * convolutional encoder over each map's fields and the rotational
+ * correlation of the two feature fields at zero translation, which orders
+ * the angle grid so that vesper_search correlates only its best fraction.
+ * Activations are float32 [C][d][d][d]; W is bfloat16 [cout][cin][3][3][3]
+ * (zero padding), accumulation in float32.
+ * ------------------------------------------------------------------------- */
+int vesper_prop_conv_fwd(const float *in, int cin, const void *W, const float *bias, int cout, int d, int relu,
+                         float *out, void *stream);
+/* Backward of one layer: din (NULL for the first layer) = input gradient;
+ * dW, db ACCUMULATE (+=).  out is the layer's forward output (ReLU mask). */
+int vesper_prop_conv_bwd(const float *dout, const float *out, int relu, const float *in, const void *W, int cin,
+                         int cout, int d, float *din, float *dW, float *db, void *stream);
+/* scores[r] = sum_k sum_v ET[k][v] * EQ[k][src_r(v)], src_r the reference's
+ * nearest-voxel rotation gather (every in-bounds voxel accepted). */
+int vesper_prop_score(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
+                      float *scores, void *stream);
+int vesper_prop_score_bwd_workspace(int K, int d, size_t *bytes);
+/* Gradients of sum_r gscores[r] * scores[r]; gET, gEQ ACCUMULATE (+=). */
+int vesper_prop_score_bwd(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
+                          const float *gscores, float *gET, float *gEQ, void *workspace, size_t workspace_bytes,
+                          void *stream);
+/* p = softmax(scores / tau): loss += -sum target log p (DEVICE float[1]),
+ * gscores = (p - target) / tau. */
+int vesper_prop_softmax_ce(const float *scores, const float *target, int n, float tau, float *loss, float *gscores,
+                           void *stream);
+/* Adam step on float32 master weights (gradient scaled by gscale), refreshing
+ * the bfloat16 copy wbf16 when non-NULL. */
+int vesper_prop_adam(float *w, float *m, float *v, const float *g, int n, float lr, float b1, float b2, float eps,
+                     int step, float gscale, void *wbf16, void *stream);
+/* idx_out int32[k]: indices of the k largest scores (ties to the lower index),
+ * those above the k-th value first, each group in index order. */
+int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void *stream);
 
 #ifdef __cplusplus
 }

@@ -288,3 +288,27 @@ def test_topn_stable_ties(dev):
     assert list(out) == [1, 2, 4, 3, 6, 0]
     out = vg.topn_device(torch.as_tensor(s).to(dev.device), 9, dev=dev).cpu().numpy()
     assert list(out) == [1, 2, 4, 3, 6, 0, 5, -1, -1]
+
+
+@pytest.mark.parametrize("d,stride", [(13, 1), (75, 97)])
+def test_register_fft_path_vs_oracle_and_radix_path(dev, d, stride):
+    """The register two-step passes (compiled for these sides in mode V)
+    against the oracle and against the radix-stage passes."""
+    vg = _vg()
+    rng = np.random.default_rng(500 + d)
+    tdata, tvec = small_field(rng, d, zero_frac=0.7)
+    qdata, qvec = small_field(rng, d, zero_frac=0.7)
+    angles = orc.calc_angle_comb(30.0)[::stride]
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), "VecProduct", 0.0, dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(angles))
+    qd, qv = dev.to_dev(qdata), dev.to_dev(qvec)
+    out = {}
+    for path in (0, 1):
+        sc, ln = vg.search_device(spec, qd, qv, "VecProduct", 0.0, mats, dev=dev, opts=(path, 0, 0))
+        out[path] = (sc[:, 0].cpu().numpy().astype(np.float64), ln[:, 0].cpu().numpy())
+    ts = orc.target_spectra(orc.mode_field("V", tdata, tvec))
+    osc, otr = orc.search(ts, "V", qdata, qvec, angles, 0.0)
+    for path in (0, 1):
+        mism = _check_search(out[path][0], out[path][1], osc.astype(np.float64), otr, d)
+        assert len(mism) <= 1, path
+    assert np.max(np.abs(out[0][0] - out[1][0])) <= SCORE_RTOL * np.max(np.abs(osc))

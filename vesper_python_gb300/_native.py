@@ -113,11 +113,22 @@ SIGNATURES = {
     "vesper_search_nscore": [_i, _i],
     "vesper_search_workspace_size": [_i, _i, _i, _i, _psz],
     "vesper_search": [_vp, _vp, _vp, _vp, _i, _i, _d, _vp, _i, _vp, _vp, _vp, _i, _vp, _sz, _vp],
-    "vesper_search_profile": [_vp, _vp, _vp, _vp, _i, _i, _d, _vp, _i, _vp, _vp, _vp, _i, _vp, _sz, _vp, _vp, _vp],
+    "vesper_search_profile": [_vp, _vp, _vp, _vp, _i, _i, _d, _vp, _i, _vp, _vp, _vp, _i, _vp, _sz, _vp, _vp, _vp,
+                              _vp],
+    "vesper_search_tuned": [_vp, _vp, _vp, _vp, _i, _i, _d, _vp, _i, _vp, _vp, _vp, _i, _vp, _sz, _vp, _vp],
     "vesper_search_static": [_vp, _vp, _vp, _vp, _i, _i, _d, _vp, _i, _vp, _vp, _vp, _vp],
     "vesper_topn": [_vp, _i, _i, _i, _vp, _vp],
     "vesper_rescore_workspace_size": [_i, _psz],
     "vesper_rescore": [_vp, _vp, _d, _d, _d, _vp, _vp, _i, _vp, _vp, _vp, _vp, _sz, _vp],
+    "vesper_prop_conv_fwd": [_vp, _i, _vp, _vp, _i, _i, _i, _vp, _vp],
+    "vesper_prop_conv_bwd": [_vp, _vp, _i, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp],
+    "vesper_prop_score": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
+    "vesper_prop_score_bwd_workspace": [_i, _i, _psz],
+    "vesper_prop_score_bwd": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp, _vp, _vp, _sz, _vp],
+    "vesper_prop_softmax_ce": [_vp, _vp, _i, ctypes.c_float, _vp, _vp, _vp],
+    "vesper_prop_adam": [_vp, _vp, _vp, _vp, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _i,
+                         ctypes.c_float, _vp, _vp],
+    "vesper_topk_subset": [_vp, _i, _i, _vp, _vp],
 }
 
 

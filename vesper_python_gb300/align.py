@@ -131,7 +131,7 @@ class Aligner:
         angle_comb = vg.calc_angle_comb(p.A)
         mats = vg.rot_matrices_device(angle_comb, dev, key=("grid", float(p.A)))
         scores, lin = vg.search_device(spec, qdata, qvec, mode, ave, mats, batch=p.batch, dev=dev,
-                                       profile=self.profile)
+                                       profile=self.profile, tuned=True)
         self.launches += self._search_launches(dim, mode, len(angle_comb), p.batch)
         top = vg.topn_device(scores, p.N, dev=dev)
         self.launches += 1
@@ -154,7 +154,7 @@ class Aligner:
         if p.A > 5.0:
             ref_angles = vg.refine_angle_list([angle_comb[r] for r in top_h])
             rmats = dev.to_dev(vg.rot_matrices(ref_angles))
-            rs, rl = vg.search_device(spec, qdata, qvec, mode, ave, rmats, batch=p.batch, dev=dev)
+            rs, rl = vg.search_device(spec, qdata, qvec, mode, ave, rmats, batch=p.batch, dev=dev, tuned=True)
             self.launches += self._search_launches(dim, mode, len(ref_angles), p.batch)
             rtop = vg.topn_device(rs, p.N, dev=dev)
             self.launches += 1
@@ -194,6 +194,11 @@ class Aligner:
 
     def _search_launches(self, dim, mode, nrot, batch):
         code = vg.MODE_CODES[mode]
+        if batch <= 0:
+            from . import autotune
+            t = autotune.cached(dim, mode, self.dev)
+            if t and t.get("batch"):
+                batch = int(t["batch"])
         if batch <= 0:
             H = dim // 2 + 1
             nch = 3 if code == 0 else (7 if code == 5 else 1)

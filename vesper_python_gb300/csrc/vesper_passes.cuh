@@ -100,6 +100,60 @@ __device__ __forceinline__ float4 gather_probs(const float *F, int d, int x, int
     return o;
 }
 
+// Single-candidate shortcut of gather_cands: the source new_pos index that
+// lands on destination t, -1 for none, -2 when two rows land there (odd d,
+// t = (d-1)/2) and the general enumeration is needed.
+__device__ __forceinline__ int cand1(int t, int d) {
+    if ((d & 1) == 0) return t;
+    const int m = (d - 1) >> 1;
+    if (t < m) return t;
+    if (t == m) return -2;
+    return t < d - 1 ? t + 1 : -1;
+}
+
+// gather4 with the rotation matrix in registers and the common case (one
+// candidate row per axis) done without the candidate loops.
+__device__ __forceinline__ int gather4_fast(const float (&F)[9], int d, int x, int y, int z, const float4 *q4,
+                                            float4 &out) {
+    const int ix = cand1(x, d), iy = cand1(y, d), iz = cand1(z, d);
+    if ((ix | iy | iz) < 0) {
+        if (ix == -1 || iy == -1 || iz == -1) return -1;
+        return gather4(F, d, x, y, z, q4, out);
+    }
+    const float hc = 0.5f * (float)d;
+    int ox, oy, oz;
+    if (!old_index(F, d, hc, (float)ix - hc, (float)iy - hc, (float)iz - hc, ox, oy, oz)) return -1;
+    const int i = (ox * d + oy) * d + oz;
+    const float4 v = q4[i];
+    if (v.w == 0.f) return -1;
+    out = v;
+    return i;
+}
+
+template <int MODE>
+__device__ __forceinline__ void sample(const Src &s, const float *F, int x, int y, int z, float *out);
+
+// Channel values of the rotated query at (x, y, z), rotation matrix in
+// registers; same results as sample().
+template <int MODE>
+__device__ __forceinline__ void sample_fast(const Src &s, const float (&F)[9], int x, int y, int z, float *out) {
+    if (MODE == VESPER_MODE_LAPLACIAN || MODE == VESPER_MODE_PROB) {
+        sample<MODE>(s, F, x, y, z, out);
+        return;
+    }
+    float4 v;
+    const bool hit = gather4_fast(F, s.d, x, y, z, s.q4, v) >= 0;
+    if (MODE == VESPER_MODE_VEC) {
+        float r[3] = {0.f, 0.f, 0.f};
+        if (hit) rotate_vec(F, v.x, v.y, v.z, r);
+        out[0] = r[0];
+        out[1] = r[1];
+        out[2] = r[2];
+    } else {
+        out[0] = hit ? v.x : 0.f;
+    }
+}
+
 // Channel values of the rotated query at (x, y, z): out[c] for every channel.
 template <int MODE>
 __device__ __forceinline__ void sample(const Src &s, const float *F, int x, int y, int z, float *out) {
@@ -213,15 +267,18 @@ __global__ void __launch_bounds__(512) k_pass_a(const PassA2 a) {
     if (threadIdx.x < 9) F[threadIdx.x] = a.rotmats[(size_t)r * 9 + threadIdx.x];
     if (x == 0 && threadIdx.x < a.nscore) a.keys[(size_t)r * a.nscore + threadIdx.x] = 0ull;
     __syncthreads();
+    float Fr[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fr[i] = F[i];
     for (int c0 = 0; c0 < NCH; c0 += a.cchunk) {
         const int cn = min(a.cchunk, NCH - c0);
         // gather two rows (2p, 2p+1) per item into packed z lines, digit-reversed z
         for (Walk2 w(d); w.o < np; w.next()) {
             const int p = w.o, z = w.i, y0 = 2 * p;
             float v0[NCH], v1[NCH];
-            sample<MODE>(a.src, F, x, y0, z, v0);
+            sample_fast<MODE>(a.src, Fr, x, y0, z, v0);
             if (y0 + 1 < d) {
-                sample<MODE>(a.src, F, x, y0 + 1, z, v1);
+                sample_fast<MODE>(a.src, Fr, x, y0 + 1, z, v1);
             } else {
 #pragma unroll
                 for (int c = 0; c < NCH; ++c) v1[c] = 0.f;

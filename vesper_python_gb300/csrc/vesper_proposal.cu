@@ -1,0 +1,403 @@
+// Learned rotation proposal: a small 3-D convolutional encoder applied to the
+// target and the query vector fields, a rotational correlation of the two
+// feature fields at zero translation over the angle grid, and the kernels to
+// train it (backward passes, softmax cross-entropy, Adam).  Nothing in the
+// reference corresponds to this: it orders the rotation grid so that only its
+// best-scored fraction is correlated by vesper_search.
+//
+// Layouts: activations [C][d][d][d] float32 (channel-major); weights
+// [Cout][Cin][27] stored as bfloat16 (3x3x3 taps, z fastest) with float32
+// accumulation; biases float32.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "vesper_common.cuh"
+
+namespace vg {
+
+// ---- convolution (3x3x3, zero padding) ----------------------------------------
+__global__ void k_conv_fwd(const float *in, int cin, const __nv_bfloat16 *W, const float *bias, int cout, int d,
+                           int relu, float *out) {
+    const int n = d * d * d;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int co = blockIdx.y;
+    if (v >= n) return;
+    const int x = v / (d * d), y = (v / d) % d, z = v % d;
+    float acc = bias ? bias[co] : 0.f;
+    const __nv_bfloat16 *w = W + (size_t)co * cin * 27;
+    for (int ci = 0; ci < cin; ++ci) {
+        const float *src = in + (size_t)ci * n;
+        const __nv_bfloat16 *wc = w + ci * 27;
+#pragma unroll
+        for (int o = 0; o < 27; ++o) {
+            const int xx = x + o / 9 - 1, yy = y + (o / 3) % 3 - 1, zz = z + o % 3 - 1;
+            if (xx < 0 || yy < 0 || zz < 0 || xx >= d || yy >= d || zz >= d) continue;
+            acc = fmaf(__bfloat162float(wc[o]), src[(xx * d + yy) * d + zz], acc);
+        }
+    }
+    out[(size_t)co * n + v] = relu ? fmaxf(acc, 0.f) : acc;
+}
+
+// din[ci][v] = sum_co sum_o W[co][ci][o] * g[co][v - o],  g = dout (masked by
+// out > 0 for a ReLU layer)
+__global__ void k_conv_bwd_data(const float *dout, const float *out, int relu, const __nv_bfloat16 *W, int cin,
+                                int cout, int d, float *din) {
+    const int n = d * d * d;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ci = blockIdx.y;
+    if (v >= n) return;
+    const int x = v / (d * d), y = (v / d) % d, z = v % d;
+    float acc = 0.f;
+    for (int co = 0; co < cout; ++co) {
+        const float *g = dout + (size_t)co * n;
+        const float *o_ = out + (size_t)co * n;
+        const __nv_bfloat16 *wc = W + ((size_t)co * cin + ci) * 27;
+#pragma unroll
+        for (int o = 0; o < 27; ++o) {
+            const int xx = x - (o / 9 - 1), yy = y - ((o / 3) % 3 - 1), zz = z - (o % 3 - 1);
+            if (xx < 0 || yy < 0 || zz < 0 || xx >= d || yy >= d || zz >= d) continue;
+            const int u = (xx * d + yy) * d + zz;
+            const float gv = (relu && !(o_[u] > 0.f)) ? 0.f : g[u];
+            acc = fmaf(__bfloat162float(wc[o]), gv, acc);
+        }
+    }
+    din[(size_t)ci * n + v] = acc;
+}
+
+// dW[co][ci][o] += sum_v g[co][v] * in[ci][v + o]; db[co] += sum_v g[co][v].
+// One block per (co, ci); 27 taps reduced over the voxels.
+__global__ void k_conv_bwd_weight(const float *dout, const float *out, int relu, const float *in, int cin, int cout,
+                                  int d, float *dW, float *db) {
+    const int n = d * d * d;
+    const int co = blockIdx.x / cin, ci = blockIdx.x % cin;
+    __shared__ float red[28][32];
+    float acc[28];
+#pragma unroll
+    for (int o = 0; o < 28; ++o) acc[o] = 0.f;
+    const float *g = dout + (size_t)co * n;
+    const float *o_ = out + (size_t)co * n;
+    const float *src = in + (size_t)ci * n;
+    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+        const float gv = (relu && !(o_[v] > 0.f)) ? 0.f : g[v];
+        if (gv == 0.f) continue;
+        const int x = v / (d * d), y = (v / d) % d, z = v % d;
+#pragma unroll
+        for (int o = 0; o < 27; ++o) {
+            const int xx = x + o / 9 - 1, yy = y + (o / 3) % 3 - 1, zz = z + o % 3 - 1;
+            if (xx < 0 || yy < 0 || zz < 0 || xx >= d || yy >= d || zz >= d) continue;
+            acc[o] = fmaf(gv, src[(xx * d + yy) * d + zz], acc[o]);
+        }
+        acc[27] += gv;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 0; o < 28; ++o) {
+        float s = acc[o];
+        for (int k = 16; k > 0; k >>= 1) s += __shfl_down_sync(0xffffffffu, s, k);
+        if (lane == 0) red[o][warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 28) {
+        float s = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+        if (threadIdx.x < 27)
+            dW[((size_t)co * cin + ci) * 27 + threadIdx.x] += s;
+        else if (ci == 0)
+            db[co] += s;
+    }
+}
+
+// ---- rotational correlation at zero translation --------------------------------
+// Source voxel of destination v under rotation F: the reference's gather rule
+// (gather_src) with every in-bounds voxel accepted.
+__device__ __forceinline__ int prop_src(const float *F, int d, int v) {
+    const int x = v / (d * d), y = (v / d) % d, z = v % d;
+    return gather_src(F, d, x, y, z, [](int) { return true; });
+}
+
+// s[r] = sum_v sum_k ET[k][v] * EQ[k][src_r(v)]; one block per rotation.
+__global__ void k_prop_score(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
+                             float *scores) {
+    __shared__ float F[9];
+    __shared__ float red[32];
+    const int r = blockIdx.x;
+    if (threadIdx.x < 9) F[threadIdx.x] = rotmats[(size_t)r * 9 + threadIdx.x];
+    __syncthreads();
+    const int n = d * d * d;
+    float acc = 0.f;
+    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+        const int s = prop_src(F, d, v);
+        if (s < 0) continue;
+        for (int k = 0; k < K; ++k) acc = fmaf(ET[(size_t)k * n + v], EQ[(size_t)k * n + s], acc);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        scores[r] = s;
+    }
+}
+
+// Partial gradients of the correlation: block b takes rotations
+// [b*chunk, (b+1)*chunk) and writes part[b][0][K][N] = sum_r g_r EQ[src_r(v)]
+// and part[b][1][K][N] = sum_r g_r scatter(ET) into the query voxels.
+__global__ void k_prop_score_bwd(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
+                                 const float *gs, int chunk, float *part) {
+    extern __shared__ __align__(16) float sm[];
+    const int n = d * d * d;
+    float *gT = sm;            // [K][n]
+    float *gQ = sm + K * n;    // [K][n]
+    __shared__ float F[9];
+    for (int i = threadIdx.x; i < 2 * K * n; i += blockDim.x) sm[i] = 0.f;
+    const int r0 = blockIdx.x * chunk, r1 = min(nrot, r0 + chunk);
+    for (int r = r0; r < r1; ++r) {
+        __syncthreads();
+        if (threadIdx.x < 9) F[threadIdx.x] = rotmats[(size_t)r * 9 + threadIdx.x];
+        __syncthreads();
+        const float g = gs[r];
+        if (g == 0.f) continue;
+        for (int v = threadIdx.x; v < n; v += blockDim.x) {
+            const int s = prop_src(F, d, v);
+            if (s < 0) continue;
+            for (int k = 0; k < K; ++k) {
+                gT[k * n + v] = fmaf(g, EQ[(size_t)k * n + s], gT[k * n + v]);
+                atomicAdd(&gQ[k * n + s], g * ET[(size_t)k * n + v]);
+            }
+        }
+    }
+    __syncthreads();
+    float *dst = part + (size_t)blockIdx.x * 2 * K * n;
+    for (int i = threadIdx.x; i < 2 * K * n; i += blockDim.x) dst[i] = sm[i];
+}
+
+__global__ void k_sum_parts(const float *part, int nparts, int len, float *out_a, float *out_b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * len) return;
+    float s = 0.f;
+    for (int p = 0; p < nparts; ++p) s += part[(size_t)p * 2 * len + i];
+    if (i < len)
+        out_a[i] += s;
+    else
+        out_b[i - len] += s;
+}
+
+// ---- loss ---------------------------------------------------------------------
+// p = softmax(s / tau); loss = -sum q log p; g = (p - q) / tau.  One block.
+__global__ void k_softmax_ce(const float *s, const float *q, int n, float tau, float *loss, float *g) {
+    __shared__ float red[32];
+    __shared__ float bc;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float m = -INFINITY;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, s[i] / tau);
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if (lane == 0) red[warp] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = -INFINITY;
+        for (int w = 0; w < nw; ++w) t = fmaxf(t, red[w]);
+        bc = t;
+    }
+    __syncthreads();
+    m = bc;
+    float z = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) z += expf(s[i] / tau - m);
+    for (int o = 16; o > 0; o >>= 1) z += __shfl_down_sync(0xffffffffu, z, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = z;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < nw; ++w) t += red[w];
+        bc = t;
+    }
+    __syncthreads();
+    const float lz = logf(bc);
+    float l = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float lp = s[i] / tau - m - lz;
+        l -= q[i] * lp;
+        g[i] = (expf(lp) - q[i]) / tau;
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < nw; ++w) t += red[w];
+        *loss += t;
+    }
+}
+
+// ---- Adam (float32 master weights, bfloat16 copies for the convolutions) ------
+__global__ void k_adam(float *w, float *m, float *v, const float *g, int n, float lr, float b1, float b2, float eps,
+                       float c1, float c2, float gscale, __nv_bfloat16 *wbf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * gscale;
+    m[i] = b1 * m[i] + (1.f - b1) * gi;
+    v[i] = b2 * v[i] + (1.f - b2) * gi * gi;
+    w[i] -= lr * (m[i] / c1) / (sqrtf(v[i] / c2) + eps);
+    if (wbf) wbf[i] = __float2bfloat16(w[i]);
+}
+
+// ---- top-k subset: indices of the k largest scores (ties to lower index) --------
+// One block: bisection on the order-preserving bit pattern for the k-th
+// largest value, then an ordered compaction.
+__global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int k, int32_t *idx) {
+    __shared__ unsigned int cnt;
+    __shared__ int ncount[1024 / 32];
+    uint32_t lo = 0u, hi = 0xffffffffu;   // answer in [lo, hi]: count(key >= t) >= k
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo + 1) / 2;
+        if (threadIdx.x == 0) cnt = 0u;
+        __syncthreads();
+        unsigned int c = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) c += float_order(s[i]) >= mid;
+        atomicAdd(&cnt, c);
+        __syncthreads();
+        if (cnt >= (unsigned)k)
+            lo = mid;
+        else
+            hi = mid - 1;
+        __syncthreads();
+    }
+    const uint32_t t = lo;
+    // strictly above the threshold first, then ties in index order, k in total
+    if (threadIdx.x == 0) cnt = 0u;
+    __syncthreads();
+    unsigned int above = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) above += float_order(s[i]) > t;
+    atomicAdd(&cnt, above);
+    __syncthreads();
+    const int n_above = (int)cnt;
+    // ordered compaction with a block-wide prefix over fixed-size tiles
+    int base_above = 0, base_tie = 0;
+    for (int start = 0; start < n; start += blockDim.x) {
+        const int i = start + threadIdx.x;
+        const uint32_t key = i < n ? float_order(s[i]) : 0u;
+        const int is_above = i < n && key > t, is_tie = i < n && key == t;
+        // warp-level ballots then a per-warp prefix
+        const unsigned ma = __ballot_sync(0xffffffffu, is_above), mt = __ballot_sync(0xffffffffu, is_tie);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0) ncount[warp] = (__popc(ma) << 16) | __popc(mt);
+        __syncthreads();
+        int pa = 0, pt = 0;
+        for (int w = 0; w < warp; ++w) {
+            pa += ncount[w] >> 16;
+            pt += ncount[w] & 0xffff;
+        }
+        const unsigned lower = (1u << lane) - 1u;
+        if (is_above) idx[base_above + pa + __popc(ma & lower)] = i;
+        if (is_tie) {
+            const int pos = base_tie + pt + __popc(mt & lower);
+            if (n_above + pos < k) idx[n_above + pos] = i;
+        }
+        int ta = 0, tt = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            ta += ncount[w] >> 16;
+            tt += ncount[w] & 0xffff;
+        }
+        base_above += ta;
+        base_tie += tt;
+        __syncthreads();
+    }
+}
+
+}  // namespace vg
+
+using namespace vg;
+
+extern "C" int vesper_prop_conv_fwd(const float *in, int cin, const void *W, const float *bias, int cout, int d,
+                                    int relu, float *out, void *stream) {
+    if (!in || !W || !out || cin < 1 || cout < 1 || d < 1) return fail(VESPER_ERR_INVALID, "conv_fwd: bad args");
+    const int n = d * d * d;
+    k_conv_fwd<<<dim3((n + 127) / 128, cout), 128, 0, (cudaStream_t)stream>>>(
+        in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
+    VG_CHECK_LAUNCH("k_conv_fwd");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_conv_bwd(const float *dout, const float *out, int relu, const float *in, const void *W,
+                                    int cin, int cout, int d, float *din, float *dW, float *db, void *stream) {
+    if (!dout || !out || !in || !W || !dW || !db || cin < 1 || cout < 1 || d < 1)
+        return fail(VESPER_ERR_INVALID, "conv_bwd: bad args");
+    const int n = d * d * d;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (din) {
+        k_conv_bwd_data<<<dim3((n + 127) / 128, cin), 128, 0, st>>>(dout, out, relu, (const __nv_bfloat16 *)W, cin,
+                                                                    cout, d, din);
+        VG_CHECK_LAUNCH("k_conv_bwd_data");
+    }
+    k_conv_bwd_weight<<<cout * cin, 256, 0, st>>>(dout, out, relu, in, cin, cout, d, dW, db);
+    VG_CHECK_LAUNCH("k_conv_bwd_weight");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_score(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
+                                 float *scores, void *stream) {
+    if (!ET || !EQ || !rotmats || !scores || K < 1 || d < 1 || nrot < 0)
+        return fail(VESPER_ERR_INVALID, "prop_score: bad args");
+    if (nrot == 0) return VESPER_OK;
+    k_prop_score<<<nrot, 256, 0, (cudaStream_t)stream>>>(ET, EQ, K, d, rotmats, nrot, scores);
+    VG_CHECK_LAUNCH("k_prop_score");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_score_bwd_workspace(int K, int d, size_t *bytes) {
+    if (!bytes) return fail(VESPER_ERR_INVALID, "bytes is NULL");
+    *bytes = (size_t)304 * 2 * K * d * d * d * sizeof(float);
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_score_bwd(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
+                                     const float *gscores, float *gET, float *gEQ, void *workspace,
+                                     size_t workspace_bytes, void *stream) {
+    const int n = d * d * d;
+    const size_t sm = (size_t)2 * K * n * sizeof(float);
+    if (!ET || !EQ || !rotmats || !gscores || !gET || !gEQ || K < 1 || d < 1 || nrot < 1)
+        return fail(VESPER_ERR_INVALID, "prop_score_bwd: bad args");
+    if (sm > (size_t)smem_limit()) return fail(VESPER_ERR_UNSUPPORTED, "prop_score_bwd: K*d^3 too large");
+    const int nblk = std::min(304, nrot);
+    const int chunk = (nrot + nblk - 1) / nblk;
+    size_t need = 0;
+    vesper_prop_score_bwd_workspace(K, d, &need);
+    if (!workspace || workspace_bytes < need) return fail(VESPER_ERR_WORKSPACE, "prop_score_bwd: workspace");
+    cudaStream_t st = (cudaStream_t)stream;
+    allow_smem(k_prop_score_bwd, sm);
+    k_prop_score_bwd<<<nblk, 256, sm, st>>>(ET, EQ, K, d, rotmats, nrot, gscores, chunk, (float *)workspace);
+    VG_CHECK_LAUNCH("k_prop_score_bwd");
+    const int len = K * n;
+    k_sum_parts<<<(2 * len + 255) / 256, 256, 0, st>>>((const float *)workspace, nblk, len, gET, gEQ);
+    VG_CHECK_LAUNCH("k_sum_parts");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_softmax_ce(const float *scores, const float *target, int n, float tau, float *loss,
+                                      float *gscores, void *stream) {
+    if (!scores || !target || !loss || !gscores || n < 1 || !(tau > 0))
+        return fail(VESPER_ERR_INVALID, "softmax_ce: bad args");
+    k_softmax_ce<<<1, 1024, 0, (cudaStream_t)stream>>>(scores, target, n, tau, loss, gscores);
+    VG_CHECK_LAUNCH("k_softmax_ce");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_adam(float *w, float *m, float *v, const float *g, int n, float lr, float b1, float b2,
+                                float eps, int step, float gscale, void *wbf16, void *stream) {
+    if (!w || !m || !v || !g || n < 0 || step < 1) return fail(VESPER_ERR_INVALID, "adam: bad args");
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    k_adam<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(w, m, v, g, n, lr, b1, b2, eps, c1, c2, gscale,
+                                                              (__nv_bfloat16 *)wbf16);
+    VG_CHECK_LAUNCH("k_adam");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void *stream) {
+    if (!scores || !idx_out || n < 1 || k < 1 || k > n) return fail(VESPER_ERR_INVALID, "topk_subset: bad args");
+    k_topk_subset<<<1, 1024, 0, (cudaStream_t)stream>>>(scores, n, k, idx_out);
+    VG_CHECK_LAUNCH("k_topk_subset");
+    return VESPER_OK;
+}

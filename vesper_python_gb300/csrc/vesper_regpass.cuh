@@ -1,0 +1,373 @@
+// Search passes with register-resident two-step line FFTs, for grid sides
+// d = N1 * N2 compiled in (vesper_search.cu instantiates the sides it
+// supports this way; every other side uses the radix-stage passes of
+// vesper_passes.cuh).  Same inputs, outputs and layouts as those passes.
+//
+//   A  gather C channels of one x plane (two rows per packed complex z line),
+//      z R2C (step 1 in place, step 2 + unpack into the plane), y FFT (step 1
+//      in place, step 2 straight to S in global memory)
+//   B  x FFT step 1 from S in global memory, step 2 + conj(T) product summed
+//      per group in registers, inverse step 2 in registers, inverse step 1
+//      straight to U
+//   C  inverse y (step 2 from U in global memory, step 1), inverse z C2R
+//      (packing + step 2, step 1 in registers) and the argmax
+#pragma once
+
+#include "vesper_passes.cuh"
+#include "vesper_regfft.cuh"
+
+namespace vg {
+
+template <int N1, int N2>
+struct RGeom {
+    static constexpr int D = N1 * N2;
+    static constexpr int H = D / 2 + 1;
+    static constexpr int NP = (D + 1) / 2;
+    static constexpr int Zp = D | 1;
+    static constexpr int Hp = H | 1;
+};
+
+// Pass A keeps, per channel, a plane of 2*NP rows of Hp complex values: packed
+// z line p lives in the storage of rows 2p and 2p+1 (D <= 2 Hp elements) and is
+// unpacked into exactly those two rows.
+template <int N1, int N2>
+__host__ __device__ inline size_t smem_ra(int cchunk) {
+    using G = RGeom<N1, N2>;
+    return align16(G::D * sizeof(float2)) + align16(16 * sizeof(float)) +
+           (size_t)cchunk * (size_t)(2 * G::NP) * G::Hp * sizeof(float2);
+}
+template <int N1, int N2>
+__host__ __device__ inline size_t smem_rb(int nch, int ngrp, int W) {
+    using G = RGeom<N1, N2>;
+    return align16(G::D * sizeof(float2)) + (size_t)(nch + ngrp) * G::D * W * sizeof(float2);
+}
+template <int N1, int N2>
+__host__ __device__ inline size_t smem_rc(int ngrp) {
+    using G = RGeom<N1, N2>;
+    return align16(G::D * sizeof(float2)) + 2 * (size_t)ngrp * G::D * G::Hp * sizeof(float2) +
+           3 * 32 * sizeof(unsigned long long);
+}
+
+// ---------------------------------------------------------------------------
+template <int MODE, int NCH, int N1, int N2>
+__global__ void __launch_bounds__(256, 3) k_rpass_a(const PassA2 a) {
+    using G = RGeom<N1, N2>;
+    constexpr int D = G::D, H = G::H, NP = G::NP, Hp = G::Hp;
+    constexpr int PS = 2 * NP * Hp;   // plane stride per channel
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int x = blockIdx.x, b = blockIdx.y, r = a.r0 + b;
+    float2 *twn = (float2 *)smem;
+    float *F = (float *)(smem + align16(D * sizeof(float2)));
+    float2 *plane = (float2 *)(smem + align16(D * sizeof(float2)) + align16(16 * sizeof(float)));
+    twiddles_n(D, twn);
+    if (threadIdx.x < 9) F[threadIdx.x] = a.rotmats[(size_t)r * 9 + threadIdx.x];
+    if (x == 0 && threadIdx.x < a.nscore) a.keys[(size_t)r * a.nscore + threadIdx.x] = 0ull;
+    __syncthreads();
+    float Fr[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fr[i] = F[i];
+    for (int c0 = 0; c0 < NCH; c0 += a.cchunk) {
+        const int cn = min(a.cchunk, NCH - c0);
+        // gather rows (2p, 2p+1) into packed z line p (natural z order)
+        for (Walk2 w(D); w.o < NP; w.next()) {
+            const int p = w.o, z = w.i, y0 = 2 * p;
+            float v0[NCH], v1[NCH];
+            sample_fast<MODE>(a.src, Fr, x, y0, z, v0);
+            if (y0 + 1 < D) {
+                sample_fast<MODE>(a.src, Fr, x, y0 + 1, z, v1);
+            } else {
+#pragma unroll
+                for (int c = 0; c < NCH; ++c) v1[c] = 0.f;
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; ++c)
+                if (c >= c0 && c < c0 + cn) plane[(c - c0) * PS + 2 * p * Hp + z] = make_float2(v0[c], v1[c]);
+        }
+        __syncthreads();
+        // z step 1, in place: items (c, j2, p), p fastest
+        for (int t = threadIdx.x; t < cn * N2 * NP; t += blockDim.x) {
+            const int p = t % NP, cj = t / NP, j2 = cj % N2, c = cj / N2;
+            float2 *line = plane + c * PS + 2 * p * Hp;
+            float2 v[N1];
+#pragma unroll
+            for (int j1 = 0; j1 < N1; ++j1) v[j1] = line[j2 + N2 * j1];
+            rdft<N1, false>(v);
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1) line[j2 + N2 * k1] = (k1 && j2) ? cmul(v[k1], twn[j2 * k1]) : v[k1];
+        }
+        __syncthreads();
+        // z step 2 + unpack into rows (2p, 2p+1), which hold line p itself: items
+        // (line, q), q in [0, N1/2]; each round covers whole lines and reads
+        // everything before it writes
+        {
+            constexpr int NQ = N1 / 2 + 1;
+            const int per_round = ((int)blockDim.x / NQ) * NQ;
+            const int items = cn * NP * NQ;
+            for (int base = 0; base < items; base += per_round) {
+                const int t = base + (int)threadIdx.x;
+                const bool on = (int)threadIdx.x < per_round && t < items;
+                const int q = t % NQ, cp = t / NQ, p = cp % NP, c = cp / NP;
+                const int q2 = (N1 - q) % N1;
+                float2 u[N2], w2[N2];
+                float2 *line = plane + c * PS + 2 * p * Hp;
+                if (on) {
+#pragma unroll
+                    for (int j2 = 0; j2 < N2; ++j2) u[j2] = line[N2 * q + j2];
+                    rdft<N2, false>(u);
+#pragma unroll
+                    for (int j2 = 0; j2 < N2; ++j2) w2[j2] = line[N2 * q2 + j2];
+                    rdft<N2, false>(w2);
+                }
+                __syncthreads();
+                if (on) {
+                    const int y = 2 * p;
+                    float2 *row0 = plane + c * PS + y * Hp;
+                    float2 *row1 = row0 + Hp;
+#pragma unroll
+                    for (int k2 = 0; k2 < N2; ++k2) {
+                        const int k = q + N1 * k2;
+                        if (k < H) {
+                            float2 A, B;
+                            unpack_pair(u[k2], (q == 0) ? u[(N2 - k2) % N2] : w2[N2 - 1 - k2], A, B);
+                            row0[k] = A;
+                            row1[k] = (y + 1 < D) ? B : make_float2(0.f, 0.f);
+                        }
+                        if (q != 0 && q2 != q) {
+                            const int kb = q2 + N1 * k2;
+                            if (kb < H) {
+                                float2 A, B;
+                                unpack_pair(w2[k2], u[N2 - 1 - k2], A, B);
+                                row0[kb] = A;
+                                row1[kb] = (y + 1 < D) ? B : make_float2(0.f, 0.f);
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // y step 1, in place: items (c, j2, kz), kz fastest
+        for (int t = threadIdx.x; t < cn * N2 * H; t += blockDim.x) {
+            const int kz = t % H, cj = t / H, j2 = cj % N2, c = cj / N2;
+            float2 *col = plane + c * PS + kz;
+            float2 v[N1];
+#pragma unroll
+            for (int j1 = 0; j1 < N1; ++j1) v[j1] = col[(j2 + N2 * j1) * Hp];
+            rdft<N1, false>(v);
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1) col[(j2 + N2 * k1) * Hp] = (k1 && j2) ? cmul(v[k1], twn[j2 * k1]) : v[k1];
+        }
+        __syncthreads();
+        // y step 2: items (c, k1, kz), kz fastest -> S rows ky = k1 + N1 k2
+        for (int t = threadIdx.x; t < cn * N1 * H; t += blockDim.x) {
+            const int kz = t % H, ck = t / H, k1 = ck % N1, c = ck / N1;
+            const float2 *col = plane + c * PS + kz;
+            float2 u[N2];
+#pragma unroll
+            for (int j2 = 0; j2 < N2; ++j2) u[j2] = col[(N2 * k1 + j2) * Hp];
+            rdft<N2, false>(u);
+            float2 *dst = a.S + (((size_t)b * NCH + c0 + c) * D + x) * (size_t)D * H + kz;
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) dst[(size_t)(k1 + N1 * k2) * H] = u[k2];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <int NCH, int NGRP, int N1, int N2>
+__global__ void __launch_bounds__(256) k_rpass_b(const PassB2 a) {
+    using G = RGeom<N1, N2>;
+    constexpr int D = G::D, H = G::H, dH = D * H;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int W = a.W, j0 = blockIdx.x * W, b = blockIdx.y;
+    float2 *twn = (float2 *)smem;
+    float2 *buf = (float2 *)(smem + align16(D * sizeof(float2)));   // [NCH][D][W]
+    float2 *pbuf = buf + (size_t)NCH * D * W;                         // [NGRP][D][W]
+    twiddles_n(D, twn);
+    __syncthreads();
+    const float2 *src = a.S + (size_t)b * NCH * D * dH;
+    // forward step 1: items (c, j2, w) from global
+    for (int t = threadIdx.x; t < NCH * N2 * W; t += blockDim.x) {
+        const int w = t % W, cj = t / W, j2 = cj % N2, c = cj / N2, j = j0 + w;
+        float2 v[N1];
+        const float2 *s = src + (size_t)c * D * dH + j;
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1) v[j1] = j < dH ? s[(size_t)(j2 + N2 * j1) * dH] : make_float2(0.f, 0.f);
+        rdft<N1, false>(v);
+        float2 *col = buf + (size_t)c * D * W + w;
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) col[(j2 + N2 * k1) * W] = (k1 && j2) ? cmul(v[k1], twn[j2 * k1]) : v[k1];
+    }
+    __syncthreads();
+    // forward step 2, product with conj(T), group sums, inverse step 2 (over
+    // k2) with conjugate twiddles into pbuf rows k1 + N1 j2: items (k1, w)
+    for (int t = threadIdx.x; t < N1 * W; t += blockDim.x) {
+        const int w = t % W, k1 = t / W, j = j0 + w;
+        float2 acc[NGRP][N2];
+#pragma unroll
+        for (int g = 0; g < NGRP; ++g)
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) acc[g][k2] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) {
+            const float2 *col = buf + (size_t)c * D * W + w;
+            float2 u[N2];
+#pragma unroll
+            for (int j2 = 0; j2 < N2; ++j2) u[j2] = col[(N2 * k1 + j2) * W];
+            rdft<N2, false>(u);
+            const int g = (NGRP == 2 && c >= 3) ? 1 : 0;
+            if (j < dH) {
+                const float2 *T = a.T + (size_t)c * D * dH + j;
+#pragma unroll
+                for (int k2 = 0; k2 < N2; ++k2)
+                    acc[g][k2] = cadd(acc[g][k2], cmul(T[(size_t)(k1 + N1 * k2) * dH], u[k2]));
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < NGRP; ++g) {
+            rdft<N2, true>(acc[g]);
+            float2 *col = pbuf + (size_t)g * D * W + w;
+#pragma unroll
+            for (int j2 = 0; j2 < N2; ++j2)
+                col[(k1 + N1 * j2) * W] = (k1 && j2) ? cmulc(acc[g][j2], twn[j2 * k1]) : acc[g][j2];
+        }
+    }
+    __syncthreads();
+    // inverse step 1: items (g, j2, w) -> U rows x = j2 + N2 j1
+    float2 *dst = a.U + (size_t)b * NGRP * D * dH;
+    for (int t = threadIdx.x; t < NGRP * N2 * W; t += blockDim.x) {
+        const int w = t % W, gj = t / W, j2 = gj % N2, g = gj / N2, j = j0 + w;
+        const float2 *col = pbuf + (size_t)g * D * W + w;
+        float2 v[N1];
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) v[k1] = col[(k1 + N1 * j2) * W];
+        rdft<N1, true>(v);
+        if (j < dH)
+#pragma unroll
+            for (int j1 = 0; j1 < N1; ++j1) dst[((size_t)g * D + j2 + N2 * j1) * dH + j] = v[j1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <int NGRP, int SC, int N1, int N2>
+__global__ void __launch_bounds__(256) k_rpass_c(const PassC2 a) {
+    using G = RGeom<N1, N2>;
+    constexpr int D = G::D, H = G::H, NP = G::NP, Zp = G::Zp, Hp = G::Hp;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int x = blockIdx.x, b = blockIdx.y, r = a.r0 + b;
+    float2 *twn = (float2 *)smem;
+    float2 *plane = (float2 *)(smem + align16(D * sizeof(float2)));   // [NGRP][D][Hp]
+    float2 *rows = plane + (size_t)NGRP * D * Hp;                      // [NGRP][D][Hp]
+    float2 *zbuf = plane;   // [NGRP][NP][Zp], NP * Zp <= D * Hp; plane is dead by then
+    unsigned long long *red = (unsigned long long *)(rows + (size_t)NGRP * D * Hp);
+    twiddles_n(D, twn);
+    __syncthreads();
+    // inverse y step 2 from U: items (g, k1, kz) -> plane rows k1 + N1 j2
+    for (int t = threadIdx.x; t < NGRP * N1 * H; t += blockDim.x) {
+        const int kz = t % H, gk = t / H, k1 = gk % N1, g = gk / N1;
+        const float2 *src = a.U + (((size_t)b * NGRP + g) * D + x) * (size_t)D * H + kz;
+        float2 u[N2];
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) u[k2] = src[(size_t)(k1 + N1 * k2) * H];
+        rdft<N2, true>(u);
+        float2 *col = plane + (size_t)g * D * Hp + kz;
+#pragma unroll
+        for (int j2 = 0; j2 < N2; ++j2) col[(k1 + N1 * j2) * Hp] = (k1 && j2) ? cmulc(u[j2], twn[j2 * k1]) : u[j2];
+    }
+    __syncthreads();
+    // inverse y step 1: items (g, j2, kz) -> rows y = j2 + N2 j1 (second buffer)
+    for (int t = threadIdx.x; t < NGRP * N2 * H; t += blockDim.x) {
+        const int kz = t % H, gj = t / H, j2 = gj % N2, g = gj / N2;
+        const float2 *col = plane + (size_t)g * D * Hp + kz;
+        float2 v[N1];
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) v[k1] = col[(k1 + N1 * j2) * Hp];
+        rdft<N1, true>(v);
+        float2 *out = rows + (size_t)g * D * Hp + kz;
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1) out[(j2 + N2 * j1) * Hp] = v[j1];
+    }
+    __syncthreads();
+    // z: pack rows (2p, 2p+1) into full lines (Hermitian completion, DC and
+    // Nyquist imaginary parts dropped), inverse step 2: items (g, p, k1)
+    for (int t = threadIdx.x; t < NGRP * NP * N1; t += blockDim.x) {
+        const int k1 = t % N1, gp = t / N1, p = gp % NP, g = gp / NP, y = 2 * p;
+        const float2 *pl = rows + (size_t)g * D * Hp;
+        const bool hb = y + 1 < D;
+        float2 u[N2];
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) {
+            const int k = k1 + N1 * k2;
+            float2 Z;
+            if (k < H) {
+                float2 A = pl[y * Hp + k], B = hb ? pl[(y + 1) * Hp + k] : make_float2(0.f, 0.f);
+                if (k == 0 || 2 * k == D) { A.y = 0.f; B.y = 0.f; }
+                Z = make_float2(A.x - B.y, A.y + B.x);
+            } else {
+                const int kk = D - k;
+                const float2 A = pl[y * Hp + kk], B = hb ? pl[(y + 1) * Hp + kk] : make_float2(0.f, 0.f);
+                Z = make_float2(A.x + B.y, B.x - A.y);
+            }
+            u[k2] = Z;
+        }
+        rdft<N2, true>(u);
+        float2 *zl = zbuf + ((size_t)g * NP + p) * Zp;
+#pragma unroll
+        for (int j2 = 0; j2 < N2; ++j2) zl[k1 + N1 * j2] = (k1 && j2) ? cmulc(u[j2], twn[j2 * k1]) : u[j2];
+    }
+    __syncthreads();
+    // inverse z step 1 + scores: items (p, j2) over every group
+    unsigned long long best[3] = {0ull, 0ull, 0ull};
+    for (int t = threadIdx.x; t < NP * N2; t += blockDim.x) {
+        const int p = t % NP, j2 = t / NP;
+        float2 v0[N1], v1[N1];
+        const float2 *zl0 = zbuf + (size_t)p * Zp;
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) v0[k1] = zl0[k1 + N1 * j2];
+        rdft<N1, true>(v0);
+        if (NGRP == 2) {
+            const float2 *zl1 = zbuf + ((size_t)NP + p) * Zp;
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1) v1[k1] = zl1[k1 + N1 * j2];
+            rdft<N1, true>(v1);
+        }
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1) {
+            const int z = j2 + N2 * j1;
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const int y = 2 * p + half;
+                if (y >= D) break;
+                const uint32_t lin = (uint32_t)((x * D + y) * D + z);
+                const float s0 = half ? v0[j1].y : v0[j1].x;
+                best[0] = max(best[0], make_key(s0, lin));
+                if (SC >= 2) {
+                    const float s1 = half ? v1[j1].y : v1[j1].x;
+                    best[1] = max(best[1], make_key(s1, lin));
+                    if (SC == 3) {
+                        const float sv = __fdiv_rn(__fsub_rn(s0, a.mix.vave), a.mix.vstd);
+                        const float sp = __fdiv_rn(__fsub_rn(s1, a.mix.pave), a.mix.pstd);
+                        const float m =
+                            __fadd_rn(__fmul_rn(a.mix.one_minus_alpha, sv), __fmul_rn(a.mix.alpha, sp));
+                        best[2] = max(best[2], make_key(m, lin));
+                    }
+                }
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int s = 0; s < SC; ++s) {
+        const unsigned long long v = warp_max_u64(best[s]);
+        if (lane == 0) red[s * 32 + warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < SC) {
+        unsigned long long v = 0ull;
+        for (int w2 = 0; w2 < nw; ++w2) v = max(v, red[threadIdx.x * 32 + w2]);
+        atomicMax(&a.keys[(size_t)r * a.nscore + threadIdx.x], v);
+    }
+}
+
+}  // namespace vg

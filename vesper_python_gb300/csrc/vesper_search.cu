@@ -16,6 +16,7 @@
 
 #include "vesper_common.cuh"
 #include "vesper_passes.cuh"
+#include "vesper_regpass.cuh"
 
 namespace vg {
 
@@ -30,7 +31,56 @@ __global__ void k_decode(const unsigned long long *keys, int n, float *scores, i
 struct SearchCfg {
     int batch, cchunk, W, threads;
     size_t sa, sb, sc;
+    int path;   // 0: radix-stage passes, 1: register two-step passes
 };
+
+// ---- register two-step passes: the sides compiled in, per mode ---------------
+struct RegEntry {
+    int mode, d;
+    size_t (*sa)(int cc);
+    size_t (*sb)(int nch, int ngrp, int W);
+    size_t (*sc)(int ngrp);
+    void (*a)(dim3, int, size_t, cudaStream_t, const PassA2 &);
+    void (*b)(dim3, int, size_t, cudaStream_t, const PassB2 &);
+    void (*c)(dim3, int, size_t, cudaStream_t, const PassC2 &, int nscore);
+};
+
+template <int MODE, int NCH, int NGRP, int N1, int N2>
+struct RegPath {
+    static void a(dim3 g, int T, size_t s, cudaStream_t st, const PassA2 &p) {
+        allow_smem(k_rpass_a<MODE, NCH, N1, N2>, s);
+        k_rpass_a<MODE, NCH, N1, N2><<<g, T, s, st>>>(p);
+    }
+    static void b(dim3 g, int T, size_t s, cudaStream_t st, const PassB2 &p) {
+        allow_smem(k_rpass_b<NCH, NGRP, N1, N2>, s);
+        k_rpass_b<NCH, NGRP, N1, N2><<<g, T, s, st>>>(p);
+    }
+    static void c(dim3 g, int T, size_t s, cudaStream_t st, const PassC2 &p, int nscore) {
+        if (NGRP == 1 || nscore == 1) {
+            allow_smem(k_rpass_c<NGRP, 1, N1, N2>, s);
+            k_rpass_c<NGRP, 1, N1, N2><<<g, T, s, st>>>(p);
+        } else if (nscore == 2) {
+            allow_smem(k_rpass_c<NGRP, 2, N1, N2>, s);
+            k_rpass_c<NGRP, 2, N1, N2><<<g, T, s, st>>>(p);
+        } else {
+            allow_smem(k_rpass_c<NGRP, 3, N1, N2>, s);
+            k_rpass_c<NGRP, 3, N1, N2><<<g, T, s, st>>>(p);
+        }
+    }
+    static RegEntry entry() {
+        return RegEntry{MODE, N1 * N2, &smem_ra<N1, N2>, &smem_rb<N1, N2>, &smem_rc<N1, N2>, &a, &b, &c};
+    }
+};
+
+static const RegEntry *find_reg(int mode, int d) {
+    static const RegEntry table[] = {
+        RegPath<VESPER_MODE_VEC, 3, 1, 25, 3>::entry(),
+        RegPath<VESPER_MODE_VEC, 3, 1, 13, 1>::entry(),
+    };
+    for (const RegEntry &e : table)
+        if (e.mode == mode && e.d == d) return &e;
+    return nullptr;
+}
 
 static int default_batch(int d, int mode) {
     const size_t H = d / 2 + 1;
@@ -136,7 +186,7 @@ extern "C" int vesper_search_workspace_size(int dim, int mode, int batch, int nr
 static int search_impl(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
                        int mode, double ave, const float *rotmats, int nrot, const double *mix, float *scores_out,
                        int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes, void *stream,
-                       PassTimer *tm) {
+                       PassTimer *tm, const int *opts = nullptr) {
     FftPlan P;
     int rc = check_dim(dim, mode, &P);
     if (rc) return rc;
@@ -155,6 +205,44 @@ static int search_impl(const void *spectra, const double *data, const float *vec
     SearchCfg cfg;
     if (!plan_passes(dim, mode, P, &cfg))
         return fail(VESPER_ERR_UNSUPPORTED, "grid side %d does not fit shared memory", dim);
+    cfg.path = 0;
+    const RegEntry *reg = find_reg(mode, dim);
+    const int want_path = opts ? opts[0] : -1;
+    if (reg && want_path != 0) {
+        const size_t lim = (size_t)smem_limit();
+        const int nchr = mode_nch(mode), ngrr = mode_ngrp(mode);
+        int cc = 0, W = 0;
+        for (size_t cap : {lim / 2 - 1024, lim}) {
+            for (int c = nchr; c >= 1 && !cc; --c)
+                if (reg->sa(c) <= cap) cc = c;
+            if (cc) break;
+        }
+        for (int w : {32, 16, 8, 4, 2, 1})
+            if (!W && reg->sb(nchr, ngrr, w) <= lim / 2 - 1024) W = w;
+        if (opts && opts[1] > 0 && opts[1] <= nchr && reg->sa(opts[1]) <= lim) cc = opts[1];
+        if (opts && opts[2] > 0 && reg->sb(nchr, ngrr, opts[2]) <= lim) W = opts[2];
+        if (cc && W && reg->sc(ngrr) <= lim) {
+            cfg.path = 1;
+            cfg.cchunk = cc;
+            cfg.W = W;
+            cfg.sa = reg->sa(cc);
+            cfg.sb = reg->sb(nchr, ngrr, W);
+            cfg.sc = reg->sc(ngrr);
+        }
+    } else if (opts) {
+        const int nchr = mode_nch(mode), ngrr = mode_ngrp(mode);
+        const size_t lim = (size_t)smem_limit();
+        if (opts[1] > 0 && opts[1] <= nchr && smem_a2(dim, P.ntab, opts[1]) <= lim) {
+            cfg.cchunk = opts[1];
+            cfg.sa = smem_a2(dim, P.ntab, opts[1]);
+        }
+        if (opts[2] > 0 && smem_b2(dim, P.ntab, nchr, ngrr, opts[2]) <= lim && nchr * opts[2] <= 2 * kThreads) {
+            cfg.W = opts[2];
+            cfg.sb = smem_b2(dim, P.ntab, nchr, ngrr, opts[2]);
+        }
+    }
+    if (want_path == 1 && cfg.path != 1)
+        return fail(VESPER_ERR_UNSUPPORTED, "no register-FFT passes compiled for mode %d, side %d", mode, dim);
     cudaStream_t st = (cudaStream_t)stream;
     const int H = dim / 2 + 1, nch = mode_nch(mode), ngrp = mode_ngrp(mode);
     const size_t N = (size_t)dim * dim * dim;
@@ -216,6 +304,21 @@ static int search_impl(const void *spectra, const double *data, const float *vec
         pc.r0 = r0;
         const dim3 gplane(dim, nb);
         mark(0, 0);
+        if (cfg.path == 1) {
+            reg->a(gplane, kThreads, cfg.sa, st, pa);
+            VG_CHECK_LAUNCH("k_rpass_a");
+            mark(0, 1);
+            mark(1, 0);
+            reg->b(dim3(nbx, nb), kThreads, cfg.sb, st, pb);
+            VG_CHECK_LAUNCH("k_rpass_b");
+            mark(1, 1);
+            mark(2, 0);
+            reg->c(gplane, kThreads, cfg.sc, st, pc, nscore);
+            VG_CHECK_LAUNCH("k_rpass_c");
+            mark(2, 1);
+            slot = (slot + 1) % kRing;
+            continue;
+        }
         switch (mode) {
             case VESPER_MODE_VEC: launch_a<VESPER_MODE_VEC, 3>(gplane, cfg, st, pa); break;
             case VESPER_MODE_OVERLAP: launch_a<VESPER_MODE_OVERLAP, 1>(gplane, cfg, st, pa); break;
@@ -258,11 +361,19 @@ extern "C" int vesper_search(const void *spectra, const double *data, const floa
                        workspace, workspace_bytes, stream, nullptr);
 }
 
+extern "C" int vesper_search_tuned(const void *spectra, const double *data, const float *vec, const float *probs,
+                                   int dim, int mode, double ave, const float *rotmats, int nrot, const double *mix,
+                                   float *scores_out, int32_t *lin_out, int batch, void *workspace,
+                                   size_t workspace_bytes, void *stream, const int *opts) {
+    return search_impl(spectra, data, vec, probs, dim, mode, ave, rotmats, nrot, mix, scores_out, lin_out, batch,
+                       workspace, workspace_bytes, stream, nullptr, opts);
+}
+
 extern "C" int vesper_search_profile(const void *spectra, const double *data, const float *vec, const float *probs,
                                      int dim, int mode, double ave, const float *rotmats, int nrot,
                                      const double *mix, float *scores_out, int32_t *lin_out, int batch,
                                      void *workspace, size_t workspace_bytes, void *stream, float *pass_ms,
-                                     int *pass_launches) {
+                                     int *pass_launches, const int *opts) {
     if (!pass_ms || !pass_launches) return fail(VESPER_ERR_INVALID, "vesper_search_profile: NULL timing outputs");
     static PassTimer tm;   // one profiling call at a time per process
     static bool created = false;
@@ -278,7 +389,7 @@ extern "C" int vesper_search_profile(const void *spectra, const double *data, co
         for (int p = 0; p < 4; ++p) tm.used[sl][p] = false;
     for (int p = 0; p < 4; ++p) tm.ms[p] = 0.f;
     const int rc = search_impl(spectra, data, vec, probs, dim, mode, ave, rotmats, nrot, mix, scores_out, lin_out,
-                               batch, workspace, workspace_bytes, stream, &tm);
+                               batch, workspace, workspace_bytes, stream, &tm, opts);
     for (int p = 0; p < 4; ++p) pass_ms[p] = tm.ms[p];
     if (batch <= 0) batch = default_batch(dim, mode);
     const int nb = nrot > 0 ? (nrot + batch - 1) / batch : 0;

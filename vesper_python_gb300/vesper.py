@@ -372,7 +372,8 @@ def target_spectra_device(data, vec, mode, ave, probs=None, dev=None):
     return spec
 
 
-def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, batch=0, dev=None, profile=None):
+def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, batch=0, dev=None, profile=None,
+                  opts=None, tuned=False):
     """vesper_search: (scores f32 [n][nscore], lin int32 [n][nscore]) CUDA tensors.
     With ``profile`` (a dict), vesper_search_profile runs instead and the dict
     receives the per-pass device milliseconds and launch counts."""
@@ -380,6 +381,11 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
     d = int(data.shape[0])
     code = mode if isinstance(mode, int) else MODE_CODES[mode]
     n = int(rotmats.shape[0])
+    if tuned and opts is None and batch == 0 and not isinstance(mode, int):
+        from . import autotune
+        t = autotune.tune(dev, spec, data, vec, mode, ave, rotmats, probs=probs, mix=mix)
+        batch = int(t["batch"])
+        opts = (-1, int(t["cchunk"]), int(t["W"]))
     nscore = dev.lib.vesper_search_nscore(code, 1 if mix is not None else 0)
     scores = torch.empty((n, nscore), dtype=torch.float32, device=dev.device)
     lin = torch.empty((n, nscore), dtype=torch.int32, device=dev.device)
@@ -388,15 +394,18 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
     mixarr = (ctypes.c_double * 5)(*[float(v) for v in mix]) if mix is not None else None
     args = (_ptr(spec), _ptr(data), _ptr(vec), _ptr(probs), d, code, float(ave or 0.0), _ptr(rotmats), n, mixarr,
             _ptr(scores), _ptr(lin), int(batch), _ptr(ws), ws.numel(), dev.stream)
-    if profile is None:
-        _native.check(dev.lib.vesper_search(*args))
-    else:
+    copts = (ctypes.c_int * 3)(*[int(v) for v in opts]) if opts is not None else None
+    if profile is not None:
         ms = (ctypes.c_float * 4)()
         nl = (ctypes.c_int * 4)()
-        _native.check(dev.lib.vesper_search_profile(*args, ms, nl))
+        _native.check(dev.lib.vesper_search_profile(*args, ms, nl, copts))
         for k in range(4):
             profile.setdefault("pass_ms", [0.0] * 4)[k] += ms[k]
             profile.setdefault("pass_launches", [0] * 4)[k] += nl[k]
+    elif copts is not None:
+        _native.check(dev.lib.vesper_search_tuned(*args, copts))
+    else:
+        _native.check(dev.lib.vesper_search(*args))
     return scores, lin
 
 
@@ -570,7 +579,7 @@ def search_map_fft(mrc_target, mrc_search, TopN=10, ang=30, mode="VecProduct", i
     angle_comb = calc_angle_comb(ang)
     mats = rot_matrices_device(angle_comb, dev, key=("grid", float(ang)))
     print("###Start Searching###")
-    scores, lin = search_device(spec, qdata, qvec, mode, mrc_target.ave, mats, batch=batch, dev=dev)
+    scores, lin = search_device(spec, qdata, qvec, mode, mrc_target.ave, mats, batch=batch, dev=dev, tuned=True)
     top = topn_device(scores, TopN, dev=dev)
     scale = score_scale(mode, mrc_target)
     raw = scores[:, 0].cpu().numpy()
@@ -601,7 +610,8 @@ def search_map_fft(mrc_target, mrc_search, TopN=10, ang=30, mode="VecProduct", i
     if ang > 5.0:
         refine_ang_arr = refine_angle_list([s["angle"] for s in sorted_topN])
         rmats = dev.to_dev(rot_matrices(refine_ang_arr))
-        rscores, rlin = search_device(spec, qdata, qvec, mode, mrc_target.ave, rmats, batch=batch, dev=dev)
+        rscores, rlin = search_device(spec, qdata, qvec, mode, mrc_target.ave, rmats, batch=batch, dev=dev,
+                                      tuned=True)
         rtop = [int(i) for i in topn_device(rscores, TopN, dev=dev).cpu().numpy() if i >= 0]
         rraw = rscores[:, 0].cpu().numpy()
         rlin_h = rlin[:, 0].cpu().numpy()
