@@ -156,9 +156,10 @@ int vesper_search(const void *spectra, const double *data, const float *vec, con
 
 /* vesper_search with explicit kernel choices, for the autotuner: HOST
  * opts[3] = {path (-1 automatic, 0 radix-stage passes, 1 register two-step
- * passes where compiled for this side and mode), channels per pass-A block
- * (0 automatic), columns per pass-B block (0 automatic)}.  Every choice gives
- * the same results up to float32 rounding of the FFT. */
+ * passes where compiled for this side and mode, 2 the fused single-kernel
+ * search where compiled), channels per pass-A block (0 automatic), columns
+ * per pass-B block (0 automatic)}.  Automatic picks 2, else 1, else 0.  Every
+ * choice gives the same results up to float32 rounding of the FFT. */
 int vesper_search_tuned(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
                         int mode, double ave, const float *rotmats, int nrot, const double *mix, float *scores_out,
                         int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes, void *stream,
@@ -176,6 +177,12 @@ int vesper_search_profile(const void *spectra, const double *data, const float *
                           int mode, double ave, const float *rotmats, int nrot, const double *mix,
                           float *scores_out, int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes,
                           void *stream, float *pass_ms, int *pass_launches, const int *opts);
+
+/* Which kernel family vesper_search_tuned(opts) runs for this side and mode
+ * (*path_out: 0 radix-stage, 1 register two-step, 2 fused) and how many
+ * kernel launches it makes for nrot rotations at this batch (0: default).
+ * No counterpart in the reference. */
+int vesper_search_plan(int dim, int mode, int batch, int nrot, const int *opts, int *path_out, int *launches_out);
 
 /* vesper_search without a workspace argument.  No counterpart in the
  * reference: it serves callers that cannot allocate device memory
@@ -226,6 +233,10 @@ int vesper_rescore(const double *tdata, const float *tvec, double tave, double t
  * Activations are float32 [C][d][d][d]; W is bfloat16 [cout][cin][3][3][3]
  * (zero padding), accumulation in float32.
  * ------------------------------------------------------------------------- */
+/* Network input of one map: out[4][dp][dp][dp] float32 (dp = ceil(d/pool)),
+ * the channels vx, vy, vz and (data != 0) of a fastVEC result averaged over
+ * pool^3 blocks (clipped at the grid edge). */
+int vesper_prop_field(const double *data, const float *vec, int d, int pool, float *out, void *stream);
 int vesper_prop_conv_fwd(const float *in, int cin, const void *W, const float *bias, int cout, int d, int relu,
                          float *out, void *stream);
 /* Backward of one layer: din (NULL for the first layer) = input gradient;

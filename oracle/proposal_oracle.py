@@ -3,7 +3,7 @@
 float64 numpy restatement of the proposal network's forward and backward
 passes (3x3x3 zero-padded convolutions with ReLU, rotational correlation of
 two feature fields at zero translation, softmax cross-entropy), used to check
-the GPU kernels' values and gradients.  The rotation's voxel map is the
+the GPU kernels' values and gradients.  Nothing in the product imports it.  The rotation's voxel map is the
 reference's nearest-voxel gather (rot_mrc, VESPER_1_prob_new.py:296-348) with
 every in-bounds voxel accepted.
 """
@@ -97,8 +97,15 @@ def score_bwd(ET, EQ, maps, g):
 
 
 def softmax_ce(s, q, tau):
-    z = s / tau
+    """Cross-entropy of softmax(u / tau) against q, u = the scores standardised
+    over the rotations (population std + 1e-6); returns (loss, dL/ds)."""
+    mu = s.mean()
+    sd = np.sqrt(np.mean((s - mu) ** 2)) + 1e-6
+    u = (s - mu) / sd
+    z = u / tau
     z = z - z.max()
     lp = z - np.log(np.exp(z).sum())
     p = np.exp(lp)
-    return -np.sum(q * lp), (p - q) / tau
+    gu = (p - q) / tau
+    gs = (gu - gu.mean() - u * np.mean(gu * u)) / sd
+    return -np.sum(q * lp), gs

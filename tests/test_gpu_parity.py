@@ -290,7 +290,7 @@ def test_topn_stable_ties(dev):
     assert list(out) == [1, 2, 4, 3, 6, 0, 5, -1, -1]
 
 
-@pytest.mark.parametrize("d,stride", [(13, 1), (75, 97)])
+@pytest.mark.parametrize("d,stride", [(13, 1), (28, 101), (30, 101), (32, 101), (75, 97)])
 def test_register_fft_path_vs_oracle_and_radix_path(dev, d, stride):
     """The register two-step passes (compiled for these sides in mode V)
     against the oracle and against the radix-stage passes."""
@@ -312,3 +312,53 @@ def test_register_fft_path_vs_oracle_and_radix_path(dev, d, stride):
         mism = _check_search(out[path][0], out[path][1], osc.astype(np.float64), otr, d)
         assert len(mism) <= 1, path
     assert np.max(np.abs(out[0][0] - out[1][0])) <= SCORE_RTOL * np.max(np.abs(osc))
+
+
+@pytest.mark.parametrize("d,stride", [(8, 7), (9, 7), (12, 3), (13, 1), (16, 5), (21, 11), (24, 13)])
+def test_fused_search_vs_oracle_and_pass_path(dev, d, stride):
+    """The fused single-kernel search (compiled sides, mode V) against the
+    oracle and against the radix-stage passes on the same rotations."""
+    vg = _vg()
+    assert vg.search_plan(d, "VecProduct", dev=dev)[0] == 2
+    rng = np.random.default_rng(700 + d)
+    tdata, tvec = small_field(rng, d, zero_frac=0.6)
+    qdata, qvec = small_field(rng, d, zero_frac=0.6)
+    angles = orc.calc_angle_comb(30.0)[::stride]
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), "VecProduct", 0.0, dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(angles))
+    qd, qv = dev.to_dev(qdata), dev.to_dev(qvec)
+    out = {}
+    for path in (0, 2):
+        sc, ln = vg.search_device(spec, qd, qv, "VecProduct", 0.0, mats, dev=dev, opts=(path, 0, 0))
+        out[path] = (sc[:, 0].cpu().numpy().astype(np.float64), ln[:, 0].cpu().numpy())
+    ts = orc.target_spectra(orc.mode_field("V", tdata, tvec))
+    osc, otr = orc.search(ts, "V", qdata, qvec, angles, 0.0)
+    mism = _check_search(out[2][0], out[2][1], osc.astype(np.float64), otr, d)
+    assert len(mism) <= 1
+    assert np.max(np.abs(out[0][0] - out[2][0])) <= SCORE_RTOL * np.max(np.abs(osc))
+
+
+@pytest.mark.parametrize("mode", ["O", "C", "P", "L"])
+@pytest.mark.parametrize("d", [12, 15])
+def test_fused_scalar_modes_vs_oracle(dev, mode, d):
+    """Fused single-kernel search in the scalar modes against the oracle."""
+    vg = _vg()
+    name = orc.MODES[mode]
+    assert vg.search_plan(d, name, dev=dev)[0] == 2
+    rng = np.random.default_rng(900 + d)
+    tdata, tvec = small_field(rng, d, zero_frac=0.5)
+    qdata, qvec = small_field(rng, d, zero_frac=0.5)
+    ave = float(np.mean(tdata[tdata > 0]))
+    angles = orc.calc_angle_comb(30.0)[::9]
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), name, ave, dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(angles))
+    sc, ln = vg.search_device(spec, dev.to_dev(qdata), dev.to_dev(qvec), name, ave, mats, dev=dev)
+    ts = orc.target_spectra(orc.mode_field(mode, tdata, tvec, ave))
+    osc, otr = orc.search(ts, mode, qdata, qvec, angles, ave)
+    got = sc[:, 0].cpu().numpy().astype(np.float64)
+    scale = np.max(np.abs(osc))
+    assert np.max(np.abs(got - osc)) <= SCORE_RTOL * scale
+    lin_ref = otr[:, 0] * d * d + otr[:, 1] * d + otr[:, 2]
+    mism = np.nonzero(ln[:, 0].cpu().numpy() != lin_ref)[0]
+    # Overlap scores are integer counts: translations may tie exactly
+    assert len(mism) <= (len(angles) if mode == "O" else 1)

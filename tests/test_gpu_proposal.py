@@ -1,0 +1,220 @@
+"""Learned rotation proposal: every forward and backward kernel against the
+float64 oracle (oracle/proposal_oracle.py), the top-k subset and the Adam
+update against numpy, and a short training run on pairs labelled by the
+exhaustive GPU search.
+
+Tolerances: kernels accumulate in float32 with bfloat16 weights (the oracle
+uses the same bfloat16-rounded weights in float64), so values and gradients
+are compared within 2e-4 of the largest magnitude of each tensor.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import proposal_oracle as po
+from oracle import vesper_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-4
+
+
+def _prop():
+    from vesper_python_gb300 import proposal
+    return proposal
+
+
+def _close(a, b, tol=TOL):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = max(np.max(np.abs(b)), 1e-30)
+    err = np.max(np.abs(a - b)) / scale
+    assert err <= tol, f"max rel err {err:.3g}"
+
+
+def _bf16(w):
+    return torch.as_tensor(w, dtype=torch.float32).to(torch.bfloat16).to(torch.float64).numpy()
+
+
+def _net(dev, seed=3, bias_scale=0.1):
+    net = _prop().ProposalNet(dev, seed=seed)
+    g = torch.Generator().manual_seed(seed)
+    for b in net.b:
+        b.copy_((torch.randn(b.shape, generator=g) * bias_scale).to(b.device))
+    return net
+
+
+def _layers(net):
+    return [(_bf16(net.Wbf[i].float().cpu()), net.b[i].double().cpu().numpy(), net.relu[i])
+            for i in range(len(net.W))]
+
+
+def _field(rng, d):
+    f = rng.normal(size=(4, d, d, d))
+    f[3] = (rng.random((d, d, d)) < 0.4).astype(np.float64)
+    return f
+
+
+def test_conv_forward_backward_vs_oracle(dev):
+    net = _net(dev)
+    rng = np.random.default_rng(0)
+    d = 7
+    x = _field(rng, d)
+    acts = net.encode(dev.to_dev(x, torch.float32))
+    layers = _layers(net)
+    oacts = po.encoder_fwd(x.astype(np.float32).astype(np.float64), layers)
+    for a, o in zip(acts[1:], oacts[1:]):
+        _close(a.cpu().numpy(), o)
+    g = rng.normal(size=oacts[-1].shape)
+    net.zero_grad()
+    net.encode_backward(acts, dev.to_dev(g, torch.float32))
+    og = po.encoder_bwd(oacts, layers, g)
+    for i in range(len(layers)):
+        _close(net.gW[i].cpu().numpy(), og[i][0])
+        _close(net.gb[i].cpu().numpy(), og[i][1])
+
+
+@pytest.mark.parametrize("d", [7, 8])
+def test_score_forward_backward_vs_oracle(dev, d):
+    P = _prop()
+    net = _net(dev)
+    rng = np.random.default_rng(10 + d)
+    K = 8
+    ET = rng.normal(size=(K, d, d, d))
+    EQ = rng.normal(size=(K, d, d, d))
+    angles = orc.calc_angle_comb(30.0)[::37]
+    from vesper_python_gb300 import vesper as vg
+    mats_h = vg.rot_matrices(angles)
+    mats = dev.to_dev(mats_h)
+    s = net.score(dev.to_dev(ET, torch.float32), dev.to_dev(EQ, torch.float32), mats).cpu().numpy()
+    maps = [po.src_map(d, mats_h[r].astype(np.float32)) for r in range(len(angles))]
+    e32t, e32q = ET.astype(np.float32).astype(np.float64), EQ.astype(np.float32).astype(np.float64)
+    os_ = po.score_fwd(e32t.reshape(K, -1), e32q.reshape(K, -1), maps)
+    _close(s, os_)
+    gs = rng.normal(size=len(angles))
+    gT = torch.zeros((K, d, d, d), device=dev.device)
+    gQ = torch.zeros((K, d, d, d), device=dev.device)
+    net.score_backward(dev.to_dev(ET, torch.float32), dev.to_dev(EQ, torch.float32), mats,
+                       dev.to_dev(gs, torch.float32), gT, gQ)
+    ogT, ogQ = po.score_bwd(e32t.reshape(K, -1), e32q.reshape(K, -1), maps, gs.astype(np.float32))
+    _close(gT.cpu().numpy().reshape(K, -1), ogT)
+    _close(gQ.cpu().numpy().reshape(K, -1), ogQ)
+    assert P is not None
+
+
+def test_softmax_ce_vs_oracle(dev):
+    rng = np.random.default_rng(5)
+    n = 3000
+    s = rng.normal(size=n) * 3
+    q = rng.random(n) ** 8
+    q /= q.sum()
+    lib = dev.lib
+    import ctypes
+    st = dev.to_dev(s, torch.float32)
+    qt = dev.to_dev(q, torch.float32)
+    loss = torch.zeros(1, device=dev.device)
+    g = torch.empty(n, device=dev.device)
+    from vesper_python_gb300 import _native
+    _native.check(lib.vesper_prop_softmax_ce(ctypes.c_void_p(st.data_ptr()), ctypes.c_void_p(qt.data_ptr()), n,
+                                             0.5, ctypes.c_void_p(loss.data_ptr()), ctypes.c_void_p(g.data_ptr()),
+                                             dev.stream))
+    ol, og = po.softmax_ce(s.astype(np.float32).astype(np.float64), q.astype(np.float32).astype(np.float64), 0.5)
+    assert abs(loss.item() - ol) <= 1e-4 * abs(ol)
+    _close(g.cpu().numpy(), og)
+
+
+def test_full_network_gradient_vs_oracle(dev):
+    """Loss of one pair through encoder(T), encoder(Q), rotation scores and
+    softmax-CE; every weight and bias gradient against the oracle."""
+    net = _net(dev, seed=7)
+    rng = np.random.default_rng(1)
+    d = 7
+    fT, fQ = _field(rng, d), _field(rng, d)
+    angles = orc.calc_angle_comb(30.0)[::23]
+    from vesper_python_gb300 import vesper as vg
+    mats_h = vg.rot_matrices(angles)
+    q = rng.random(len(angles)) ** 4
+    q /= q.sum()
+    tau = 0.5
+    net.zero_grad()
+    loss = net.loss_and_grad(dev.to_dev(fT, torch.float32), dev.to_dev(fQ, torch.float32), dev.to_dev(mats_h),
+                             dev.to_dev(q, torch.float32), tau)
+    layers = _layers(net)
+    f32 = lambda a: a.astype(np.float32).astype(np.float64)
+    aT = po.encoder_fwd(f32(fT), layers)
+    aQ = po.encoder_fwd(f32(fQ), layers)
+    K = aT[-1].shape[0]
+    maps = [po.src_map(d, mats_h[r].astype(np.float32)) for r in range(len(angles))]
+    s = po.score_fwd(aT[-1].reshape(K, -1), aQ[-1].reshape(K, -1), maps)
+    ol, gs = po.softmax_ce(s, f32(q), tau)
+    assert abs(loss.item() - ol) <= 1e-3 * abs(ol)
+    gT, gQ = po.score_bwd(aT[-1].reshape(K, -1), aQ[-1].reshape(K, -1), maps, gs)
+    grT = po.encoder_bwd(aT, layers, gT.reshape(aT[-1].shape))
+    grQ = po.encoder_bwd(aQ, layers, gQ.reshape(aQ[-1].shape))
+    for i in range(len(layers)):
+        _close(net.gW[i].cpu().numpy(), grT[i][0] + grQ[i][0], 1e-3)
+        _close(net.gb[i].cpu().numpy(), grT[i][1] + grQ[i][1], 1e-3)
+
+
+@pytest.mark.parametrize("n,k", [(1, 1), (100, 7), (24624, 1232), (5000, 5000)])
+def test_topk_subset(dev, n, k):
+    import ctypes
+    from vesper_python_gb300 import _native
+    rng = np.random.default_rng(n + k)
+    s = np.round(rng.normal(size=n) * 20) / 4          # many ties
+    st = dev.to_dev(s, torch.float32)
+    idx = torch.full((k,), -1, dtype=torch.int32, device=dev.device)
+    _native.check(dev.lib.vesper_topk_subset(ctypes.c_void_p(st.data_ptr()), n, k, ctypes.c_void_p(idx.data_ptr()),
+                                             dev.stream))
+    got = np.sort(idx.cpu().numpy())
+    want = np.sort(np.lexsort((np.arange(n), -s.astype(np.float32)))[:k])
+    assert np.array_equal(got, want)
+
+
+def test_adam_step(dev):
+    net = _net(dev)
+    rng = np.random.default_rng(2)
+    w0 = [w.cpu().numpy().astype(np.float64) for w in net.W]
+    grads = [rng.normal(size=w.shape) for w in w0]
+    for i, g in enumerate(grads):
+        net.gW[i].copy_(torch.as_tensor(g, dtype=torch.float32))
+        net.gb[i].zero_()
+    net.adam_step(1e-2, batch=2)
+    for i, g in enumerate(grads):
+        gi = g.astype(np.float32).astype(np.float64) * 0.5
+        m = 0.1 * gi
+        v = 0.001 * gi * gi
+        want = w0[i] - 1e-2 * (m / 0.1) / (np.sqrt(v / 0.001) + 1e-8)
+        np.testing.assert_allclose(net.W[i].cpu().numpy(), want, rtol=1e-5, atol=1e-6)
+        assert torch.equal(net.Wbf[i].cpu().float(), net.W[i].to(torch.bfloat16).cpu().float())
+
+
+def test_short_training_lowers_loss(dev):
+    """Eight config-0-style pairs labelled by the exhaustive search (A = 30);
+    a few Adam epochs on the GPU lower the training loss."""
+    P = _prop()
+    from vesper_python_gb300 import vesper as vg
+    net = P.ProposalNet(dev, seed=0)
+    mats = vg.rot_matrices_device(vg.calc_angle_comb(30.0), dev, key=("grid", 30.0))
+    hist = P.train(dev, net, list(range(8)), mats, epochs=6, batch=4, lr=3e-3)
+    assert np.all(np.isfinite(hist))
+    assert hist[-1] < hist[0]
+
+
+@pytest.mark.parametrize("d,pool", [(30, 2), (13, 2), (12, 1)])
+def test_prop_field_pooling(dev, d, pool):
+    P = _prop()
+    rng = np.random.default_rng(d)
+    data = rng.uniform(0, 1, size=(d, d, d))
+    data[data < 0.4] = 0
+    vec = rng.normal(size=(d, d, d, 3)).astype(np.float32)
+    f = P.map_field(dev.to_dev(data), dev.to_dev(vec), pool, dev).cpu().numpy()
+    dp = (d + pool - 1) // pool
+    want = np.zeros((4, dp, dp, dp))
+    full = np.concatenate([vec.astype(np.float64), (data != 0)[..., None].astype(np.float64)], axis=-1)
+    for X in range(dp):
+        for Y in range(dp):
+            for Z in range(dp):
+                blk = full[X * pool:(X + 1) * pool, Y * pool:(Y + 1) * pool, Z * pool:(Z + 1) * pool]
+                want[:, X, Y, Z] = blk.reshape(-1, 4).mean(axis=0)
+    np.testing.assert_allclose(f, want, rtol=1e-5, atol=1e-6)

@@ -116,10 +116,12 @@ SIGNATURES = {
     "vesper_search_profile": [_vp, _vp, _vp, _vp, _i, _i, _d, _vp, _i, _vp, _vp, _vp, _i, _vp, _sz, _vp, _vp, _vp,
                               _vp],
     "vesper_search_tuned": [_vp, _vp, _vp, _vp, _i, _i, _d, _vp, _i, _vp, _vp, _vp, _i, _vp, _sz, _vp, _vp],
+    "vesper_search_plan": [_i, _i, _i, _i, _vp, _vp, _vp],
     "vesper_search_static": [_vp, _vp, _vp, _vp, _i, _i, _d, _vp, _i, _vp, _vp, _vp, _vp],
     "vesper_topn": [_vp, _i, _i, _i, _vp, _vp],
     "vesper_rescore_workspace_size": [_i, _psz],
     "vesper_rescore": [_vp, _vp, _d, _d, _d, _vp, _vp, _i, _vp, _vp, _vp, _vp, _sz, _vp],
+    "vesper_prop_field": [_vp, _vp, _i, _i, _vp, _vp],
     "vesper_prop_conv_fwd": [_vp, _i, _vp, _vp, _i, _i, _i, _vp, _vp],
     "vesper_prop_conv_bwd": [_vp, _vp, _i, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp],
     "vesper_prop_score": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],

@@ -193,19 +193,12 @@ class Aligner:
         return AlignResult(dim, std_s, ave_s, top_list, models, self.launches)
 
     def _search_launches(self, dim, mode, nrot, batch):
-        code = vg.MODE_CODES[mode]
         if batch <= 0:
             from . import autotune
             t = autotune.cached(dim, mode, self.dev)
             if t and t.get("batch"):
                 batch = int(t["batch"])
-        if batch <= 0:
-            H = dim // 2 + 1
-            nch = 3 if code == 0 else (7 if code == 5 else 1)
-            ngrp = 2 if code == 5 else 1
-            per = (nch + ngrp) * dim * dim * H * 8
-            batch = max(1, min(64, (64 << 20) // per))
-        return 3 * ((nrot + batch - 1) // batch) + 1
+        return vg.search_plan(dim, mode, batch, nrot, None, self.dev)[1]
 
     def align_host(self, map1, map2, width1, width2, orig1, orig2, p: AlignParams, pinned=None):
         """End-to-end: host [x][y][z] float32 maps (pinned if given) -> results."""

@@ -3,7 +3,7 @@
 For a (grid side, mode) pair it times vesper_search_tuned over a sample of
 rotations for every candidate of
 
-  batch      rotations per pipeline step (S and U stay L2-resident up to ~16)
+  batch      rotations per pipeline step (8 to 2048, S + U of a step <= 96 MB)
   cchunk     channels gathered and transformed per pass-A block
   W          spectrum columns per pass-B block
 
@@ -62,9 +62,16 @@ def _save_disk(entries):
         pass
 
 
-def candidates(nch):
+BATCHES = (8, 16, 32, 64, 128, 256, 512, 1024, 2048)
+BATCH_BYTES = 96 << 20      # S + U of one batch, kept near the L2 size
+
+
+def candidates(nch, dim=None, ngrp=1):
+    per = None if dim is None else (nch + ngrp) * dim * dim * (dim // 2 + 1) * 8
     out = []
-    for batch in (8, 16, 32, 64):
+    for batch in BATCHES:
+        if batch > 64 and (per is None or batch * per > BATCH_BYTES):
+            continue
         for cc in sorted({1, nch}):
             for W in (16, 32):
                 out.append({"batch": batch, "cchunk": cc, "W": W})
@@ -84,10 +91,20 @@ def tune(dev, spec, data, vec, mode, ave, rotmats, probs=None, mix=None, sample=
         if key in disk:
             _mem[key] = disk[key]
             return disk[key]
-    mats = rotmats[: min(sample, rotmats.shape[0])]
+    if vg.search_plan(dim, mode, 0, 1, None, dev)[0] == 2:
+        # the fused single-kernel search has no launch shape to choose
+        best = {"batch": 0, "cchunk": 0, "W": 0, "ms_per_rot": None, "path": 2}
+        with _lock:
+            _mem[key] = best
+        return best
     nch = {"VecProduct": 3, "prob": 7}.get(mode, 1)
+    ngrp = 2 if mode == "prob" else 1
+    cands = candidates(nch, dim, ngrp)
+    # the sample covers two steps of the largest batch tried
+    sample = max(sample, 2 * max(c["batch"] for c in cands))
+    mats = rotmats[: min(sample, rotmats.shape[0])]
     best = None
-    for c in candidates(nch):
+    for c in cands:
         try:
             ms = None
             for _ in range(reps):

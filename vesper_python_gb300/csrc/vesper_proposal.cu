@@ -16,6 +16,11 @@
 
 namespace vg {
 
+// blocks of the score backward pass (two waves of the 152 SMs at most); each
+// keeps its partial gradients in shared memory and writes them to its own
+// workspace slot
+constexpr int kPropBlocks = 304;
+
 // ---- convolution (3x3x3, zero padding) ----------------------------------------
 __global__ void k_conv_fwd(const float *in, int cin, const __nv_bfloat16 *W, const float *bias, int cout, int d,
                            int relu, float *out) {
@@ -108,6 +113,32 @@ __global__ void k_conv_bwd_weight(const float *dout, const float *out, int relu,
     }
 }
 
+// ---- network input ---------------------------------------------------------------
+// out[c][X][Y][Z], c = (vx, vy, vz, mask = data != 0), each the mean over the
+// pool^3 block of voxels (pool X .. pool X + pool - 1, clipped at the grid
+// edge) of the fastVEC output of one map.
+__global__ void k_prop_field(const double *data, const float *vec, int d, int pool, int dp, float *out) {
+    const int np = dp * dp * dp;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const int X = i / (dp * dp), Y = (i / dp) % dp, Z = i % dp;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    int cnt = 0;
+    for (int x = X * pool; x < min(d, X * pool + pool); ++x)
+        for (int y = Y * pool; y < min(d, Y * pool + pool); ++y)
+            for (int z = Z * pool; z < min(d, Z * pool + pool); ++z) {
+                const size_t v = ((size_t)x * d + y) * d + z;
+                acc[0] += vec[3 * v];
+                acc[1] += vec[3 * v + 1];
+                acc[2] += vec[3 * v + 2];
+                acc[3] += data[v] != 0.0 ? 1.f : 0.f;
+                ++cnt;
+            }
+    const float inv = 1.f / (float)cnt;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) out[(size_t)c * np + i] = acc[c] * inv;
+}
+
 // ---- rotational correlation at zero translation --------------------------------
 // Source voxel of destination v under rotation F: the reference's gather rule
 // (gather_src) with every in-bounds voxel accepted.
@@ -141,17 +172,18 @@ __global__ void k_prop_score(const float *ET, const float *EQ, int K, int d, con
     }
 }
 
-// Partial gradients of the correlation: block b takes rotations
-// [b*chunk, (b+1)*chunk) and writes part[b][0][K][N] = sum_r g_r EQ[src_r(v)]
-// and part[b][1][K][N] = sum_r g_r scatter(ET) into the query voxels.
-__global__ void k_prop_score_bwd(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
-                                 const float *gs, int chunk, float *part) {
+// Partial gradients of the correlation for channels [k0, k0 + kc): block b
+// takes rotations [b*chunk, (b+1)*chunk) and writes part[b][0][k][v] =
+// sum_r g_r EQ[k][src_r(v)] and part[b][1][k][s] = sum_r g_r ET[k][v] summed
+// over the v with src_r(v) = s, accumulated in shared memory.
+__global__ void k_prop_score_bwd(const float *ET, const float *EQ, int K, int k0, int kc, int d,
+                                 const float *rotmats, int nrot, const float *gs, int chunk, float *part) {
     extern __shared__ __align__(16) float sm[];
     const int n = d * d * d;
-    float *gT = sm;            // [K][n]
-    float *gQ = sm + K * n;    // [K][n]
+    float *gT = sm;             // [kc][n]
+    float *gQ = sm + kc * n;    // [kc][n]
     __shared__ float F[9];
-    for (int i = threadIdx.x; i < 2 * K * n; i += blockDim.x) sm[i] = 0.f;
+    for (int i = threadIdx.x; i < 2 * kc * n; i += blockDim.x) sm[i] = 0.f;
     const int r0 = blockIdx.x * chunk, r1 = min(nrot, r0 + chunk);
     for (int r = r0; r < r1; ++r) {
         __syncthreads();
@@ -162,15 +194,18 @@ __global__ void k_prop_score_bwd(const float *ET, const float *EQ, int K, int d,
         for (int v = threadIdx.x; v < n; v += blockDim.x) {
             const int s = prop_src(F, d, v);
             if (s < 0) continue;
-            for (int k = 0; k < K; ++k) {
-                gT[k * n + v] = fmaf(g, EQ[(size_t)k * n + s], gT[k * n + v]);
-                atomicAdd(&gQ[k * n + s], g * ET[(size_t)k * n + v]);
+            for (int k = 0; k < kc; ++k) {
+                gT[k * n + v] = fmaf(g, EQ[(size_t)(k0 + k) * n + s], gT[k * n + v]);
+                atomicAdd(&gQ[k * n + s], g * ET[(size_t)(k0 + k) * n + v]);
             }
         }
     }
     __syncthreads();
     float *dst = part + (size_t)blockIdx.x * 2 * K * n;
-    for (int i = threadIdx.x; i < 2 * K * n; i += blockDim.x) dst[i] = sm[i];
+    for (int i = threadIdx.x; i < 2 * kc * n; i += blockDim.x) {
+        const int half = i / (kc * n), rem = i % (kc * n);
+        dst[(size_t)half * K * n + (size_t)k0 * n + rem] = sm[i];
+    }
 }
 
 __global__ void k_sum_parts(const float *part, int nparts, int len, float *out_a, float *out_b) {
@@ -185,51 +220,69 @@ __global__ void k_sum_parts(const float *part, int nparts, int len, float *out_a
 }
 
 // ---- loss ---------------------------------------------------------------------
-// p = softmax(s / tau); loss = -sum q log p; g = (p - q) / tau.  One block.
+// Block-wide sum / max of one value per thread (blockDim a multiple of 32).
+__device__ float block_sum(float v, float *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float t = 0.f;
+    for (int w = 0; w < nw; ++w) t += red[w];
+    return t;
+}
+__device__ float block_max(float v, float *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float t = -INFINITY;
+    for (int w = 0; w < nw; ++w) t = fmaxf(t, red[w]);
+    return t;
+}
+
+// Standardised scores u = (s - mean) / std over the rotations, p =
+// softmax(u / tau), loss += -sum q log p, and the gradient with respect to s
+// through the standardisation:
+//   gu = (p - q) / tau,  gs = (gu - mean(gu) - u * mean(gu * u)) / std.
+// One block; three passes over the n scores.
 __global__ void k_softmax_ce(const float *s, const float *q, int n, float tau, float *loss, float *g) {
     __shared__ float red[32];
-    __shared__ float bc;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    float m = -INFINITY;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, s[i] / tau);
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-    if (lane == 0) red[warp] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float t = -INFINITY;
-        for (int w = 0; w < nw; ++w) t = fmaxf(t, red[w]);
-        bc = t;
-    }
-    __syncthreads();
-    m = bc;
-    float z = 0.f;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) z += expf(s[i] / tau - m);
-    for (int o = 16; o > 0; o >>= 1) z += __shfl_down_sync(0xffffffffu, z, o);
-    __syncthreads();
-    if (lane == 0) red[warp] = z;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float t = 0.f;
-        for (int w = 0; w < nw; ++w) t += red[w];
-        bc = t;
-    }
-    __syncthreads();
-    const float lz = logf(bc);
-    float l = 0.f;
+    float a = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) a += s[i];
+    const float mu = block_sum(a, red) / (float)n;
+    a = 0.f;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float lp = s[i] / tau - m - lz;
+        const float t = s[i] - mu;
+        a = fmaf(t, t, a);
+    }
+    const float sd = sqrtf(block_sum(a, red) / (float)n) + 1e-6f;
+    const float inv = 1.f / sd;
+    float m = -INFINITY;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, (s[i] - mu) * inv / tau);
+    m = block_max(m, red);
+    a = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) a += expf((s[i] - mu) * inv / tau - m);
+    const float lz = logf(block_sum(a, red));
+    float l = 0.f, sg = 0.f, sgu = 0.f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float u = (s[i] - mu) * inv;
+        const float lp = u / tau - m - lz;
         l -= q[i] * lp;
-        g[i] = (expf(lp) - q[i]) / tau;
+        const float gu = (expf(lp) - q[i]) / tau;
+        g[i] = gu;
+        sg += gu;
+        sgu = fmaf(gu, u, sgu);
     }
-    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
-    __syncthreads();
-    if (lane == 0) red[warp] = l;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float t = 0.f;
-        for (int w = 0; w < nw; ++w) t += red[w];
-        *loss += t;
+    l = block_sum(l, red);
+    const float mg = block_sum(sg, red) / (float)n;
+    const float mgu = block_sum(sgu, red) / (float)n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float u = (s[i] - mu) * inv;
+        g[i] = (g[i] - mg - u * mgu) * inv;
     }
+    if (threadIdx.x == 0) *loss += l;
 }
 
 // ---- Adam (float32 master weights, bfloat16 copies for the convolutions) ------
@@ -251,8 +304,10 @@ __global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int
     __shared__ unsigned int cnt;
     __shared__ int ncount[1024 / 32];
     uint32_t lo = 0u, hi = 0xffffffffu;   // answer in [lo, hi]: count(key >= t) >= k
-    while (lo < hi) {
-        const uint32_t mid = lo + (hi - lo + 1) / 2;
+    // the interval halves every round (midpoint taken in 64 bits), so 32
+    // rounds reach lo == hi; the bound is explicit all the same
+    for (int round = 0; round < 40 && lo < hi; ++round) {
+        const uint32_t mid = (uint32_t)(((uint64_t)lo + (uint64_t)hi + 1ull) >> 1);
         if (threadIdx.x == 0) cnt = 0u;
         __syncthreads();
         unsigned int c = 0;
@@ -311,6 +366,15 @@ __global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int
 
 using namespace vg;
 
+extern "C" int vesper_prop_field(const double *data, const float *vec, int d, int pool, float *out, void *stream) {
+    if (!data || !vec || !out || d < 1 || pool < 1) return fail(VESPER_ERR_INVALID, "prop_field: bad args");
+    const int dp = (d + pool - 1) / pool;
+    const int np = dp * dp * dp;
+    k_prop_field<<<(np + 127) / 128, 128, 0, (cudaStream_t)stream>>>(data, vec, d, pool, dp, out);
+    VG_CHECK_LAUNCH("k_prop_field");
+    return VESPER_OK;
+}
+
 extern "C" int vesper_prop_conv_fwd(const float *in, int cin, const void *W, const float *bias, int cout, int d,
                                     int relu, float *out, void *stream) {
     if (!in || !W || !out || cin < 1 || cout < 1 || d < 1) return fail(VESPER_ERR_INVALID, "conv_fwd: bad args");
@@ -349,27 +413,34 @@ extern "C" int vesper_prop_score(const float *ET, const float *EQ, int K, int d,
 
 extern "C" int vesper_prop_score_bwd_workspace(int K, int d, size_t *bytes) {
     if (!bytes) return fail(VESPER_ERR_INVALID, "bytes is NULL");
-    *bytes = (size_t)304 * 2 * K * d * d * d * sizeof(float);
+    *bytes = (size_t)kPropBlocks * 2 * K * d * d * d * sizeof(float);
     return VESPER_OK;
 }
 
 extern "C" int vesper_prop_score_bwd(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
                                      const float *gscores, float *gET, float *gEQ, void *workspace,
                                      size_t workspace_bytes, void *stream) {
-    const int n = d * d * d;
-    const size_t sm = (size_t)2 * K * n * sizeof(float);
     if (!ET || !EQ || !rotmats || !gscores || !gET || !gEQ || K < 1 || d < 1 || nrot < 1)
         return fail(VESPER_ERR_INVALID, "prop_score_bwd: bad args");
-    if (sm > (size_t)smem_limit()) return fail(VESPER_ERR_UNSUPPORTED, "prop_score_bwd: K*d^3 too large");
-    const int nblk = std::min(304, nrot);
+    const int n = d * d * d;
+    // channels per launch: the largest divisor of K whose two [kc][n] float
+    // buffers fit in shared memory
+    int kc = K;
+    while (kc > 0 && (K % kc != 0 || (size_t)2 * kc * n * sizeof(float) > (size_t)smem_limit())) --kc;
+    if (kc < 1) return fail(VESPER_ERR_UNSUPPORTED, "prop_score_bwd: d^3 too large for shared memory");
+    const size_t sm = (size_t)2 * kc * n * sizeof(float);
+    const int nblk = std::min(kPropBlocks, nrot);
     const int chunk = (nrot + nblk - 1) / nblk;
     size_t need = 0;
     vesper_prop_score_bwd_workspace(K, d, &need);
     if (!workspace || workspace_bytes < need) return fail(VESPER_ERR_WORKSPACE, "prop_score_bwd: workspace");
     cudaStream_t st = (cudaStream_t)stream;
     allow_smem(k_prop_score_bwd, sm);
-    k_prop_score_bwd<<<nblk, 256, sm, st>>>(ET, EQ, K, d, rotmats, nrot, gscores, chunk, (float *)workspace);
-    VG_CHECK_LAUNCH("k_prop_score_bwd");
+    for (int k0 = 0; k0 < K; k0 += kc) {
+        k_prop_score_bwd<<<nblk, 256, sm, st>>>(ET, EQ, K, k0, kc, d, rotmats, nrot, gscores, chunk,
+                                                (float *)workspace);
+        VG_CHECK_LAUNCH("k_prop_score_bwd");
+    }
     const int len = K * n;
     k_sum_parts<<<(2 * len + 255) / 256, 256, 0, st>>>((const float *)workspace, nblk, len, gET, gEQ);
     VG_CHECK_LAUNCH("k_sum_parts");

@@ -370,4 +370,49 @@ __global__ void __launch_bounds__(256) k_rpass_c(const PassC2 a) {
     }
 }
 
+// ---- one compiled side of the register passes, as vesper_search.cu calls it ----
+struct RegEntry {
+    int mode, d;
+    size_t (*sa)(int cc);
+    size_t (*sb)(int nch, int ngrp, int W);
+    size_t (*sc)(int ngrp);
+    void (*a)(dim3, int, size_t, cudaStream_t, const PassA2 &);
+    void (*b)(dim3, int, size_t, cudaStream_t, const PassB2 &);
+    void (*c)(dim3, int, size_t, cudaStream_t, const PassC2 &, int nscore);
+};
+
+template <int MODE, int NCH, int NGRP, int N1, int N2>
+struct RegPath {
+    static void a(dim3 g, int T, size_t s, cudaStream_t st, const PassA2 &p) {
+        allow_smem(k_rpass_a<MODE, NCH, N1, N2>, s);
+        k_rpass_a<MODE, NCH, N1, N2><<<g, T, s, st>>>(p);
+    }
+    static void b(dim3 g, int T, size_t s, cudaStream_t st, const PassB2 &p) {
+        allow_smem(k_rpass_b<NCH, NGRP, N1, N2>, s);
+        k_rpass_b<NCH, NGRP, N1, N2><<<g, T, s, st>>>(p);
+    }
+    static void c(dim3 g, int T, size_t s, cudaStream_t st, const PassC2 &p, int nscore) {
+        if constexpr (NGRP == 1) {
+            allow_smem(k_rpass_c<1, 1, N1, N2>, s);
+            k_rpass_c<1, 1, N1, N2><<<g, T, s, st>>>(p);
+        } else if (nscore == 1) {
+            allow_smem(k_rpass_c<NGRP, 1, N1, N2>, s);
+            k_rpass_c<NGRP, 1, N1, N2><<<g, T, s, st>>>(p);
+        } else if (nscore == 2) {
+            allow_smem(k_rpass_c<NGRP, 2, N1, N2>, s);
+            k_rpass_c<NGRP, 2, N1, N2><<<g, T, s, st>>>(p);
+        } else {
+            allow_smem(k_rpass_c<NGRP, 3, N1, N2>, s);
+            k_rpass_c<NGRP, 3, N1, N2><<<g, T, s, st>>>(p);
+        }
+    }
+    static RegEntry entry() {
+        return RegEntry{MODE, N1 * N2, &smem_ra<N1, N2>, &smem_rb<N1, N2>, &smem_rc<N1, N2>, &a, &b, &c};
+    }
+};
+
+// Lookups of the tables in vesper_regsearch_a.cu / vesper_regsearch_b.cu.
+const RegEntry *find_reg_a(int mode, int d);
+const RegEntry *find_reg_b(int mode, int d);
+
 }  // namespace vg

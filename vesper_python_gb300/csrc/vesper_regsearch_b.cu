@@ -1,0 +1,18 @@
+// Register two-step search passes: the compiled sides, table b of two.
+// Split across translation units so that they compile in parallel.
+#define VG_PASS_TYPES_ONLY
+#include "vesper_regpass.cuh"
+
+namespace vg {
+
+const RegEntry *find_reg_b(int mode, int d) {
+    static const RegEntry table[] = {
+        RegPath<VESPER_MODE_VEC, 3, 1, 25, 3>::entry(),   // 75: 200^3 / 100^3 pairs at s = 2
+        RegPath<VESPER_MODE_VEC, 3, 1, 8, 4>::entry(),    // 32: 128^3 / 64^3 pairs at s = 3
+    };
+    for (const RegEntry &e : table)
+        if (e.mode == mode && e.d == d) return &e;
+    return nullptr;
+}
+
+}  // namespace vg

@@ -34,60 +34,20 @@ struct SearchCfg {
     int path;   // 0: radix-stage passes, 1: register two-step passes
 };
 
-// ---- register two-step passes: the sides compiled in, per mode ---------------
-struct RegEntry {
-    int mode, d;
-    size_t (*sa)(int cc);
-    size_t (*sb)(int nch, int ngrp, int W);
-    size_t (*sc)(int ngrp);
-    void (*a)(dim3, int, size_t, cudaStream_t, const PassA2 &);
-    void (*b)(dim3, int, size_t, cudaStream_t, const PassB2 &);
-    void (*c)(dim3, int, size_t, cudaStream_t, const PassC2 &, int nscore);
-};
+// ---- register two-step passes: the sides compiled in (vesper_regsearch_*.cu)
+const RegEntry *find_reg(int mode, int d);
 
-template <int MODE, int NCH, int NGRP, int N1, int N2>
-struct RegPath {
-    static void a(dim3 g, int T, size_t s, cudaStream_t st, const PassA2 &p) {
-        allow_smem(k_rpass_a<MODE, NCH, N1, N2>, s);
-        k_rpass_a<MODE, NCH, N1, N2><<<g, T, s, st>>>(p);
-    }
-    static void b(dim3 g, int T, size_t s, cudaStream_t st, const PassB2 &p) {
-        allow_smem(k_rpass_b<NCH, NGRP, N1, N2>, s);
-        k_rpass_b<NCH, NGRP, N1, N2><<<g, T, s, st>>>(p);
-    }
-    static void c(dim3 g, int T, size_t s, cudaStream_t st, const PassC2 &p, int nscore) {
-        if (NGRP == 1 || nscore == 1) {
-            allow_smem(k_rpass_c<NGRP, 1, N1, N2>, s);
-            k_rpass_c<NGRP, 1, N1, N2><<<g, T, s, st>>>(p);
-        } else if (nscore == 2) {
-            allow_smem(k_rpass_c<NGRP, 2, N1, N2>, s);
-            k_rpass_c<NGRP, 2, N1, N2><<<g, T, s, st>>>(p);
-        } else {
-            allow_smem(k_rpass_c<NGRP, 3, N1, N2>, s);
-            k_rpass_c<NGRP, 3, N1, N2><<<g, T, s, st>>>(p);
-        }
-    }
-    static RegEntry entry() {
-        return RegEntry{MODE, N1 * N2, &smem_ra<N1, N2>, &smem_rb<N1, N2>, &smem_rc<N1, N2>, &a, &b, &c};
-    }
-};
-
-static const RegEntry *find_reg(int mode, int d) {
-    static const RegEntry table[] = {
-        RegPath<VESPER_MODE_VEC, 3, 1, 25, 3>::entry(),
-        RegPath<VESPER_MODE_VEC, 3, 1, 13, 1>::entry(),
-    };
-    for (const RegEntry &e : table)
-        if (e.mode == mode && e.d == d) return &e;
-    return nullptr;
-}
+// vesper_fused.cu: 1 if a fused single-kernel search is compiled for (mode,
+// side) -- launched when rc is non-null, its status stored there -- else 0.
+int vesper_fused_search(int mode, int d, const Src &src, const float *rotmats, const void *spectra, int nrot,
+                        int nscore, unsigned long long *keys, cudaStream_t st, int *rc);
 
 static int default_batch(int d, int mode) {
     const size_t H = d / 2 + 1;
     const size_t per = (size_t)(mode_nch(mode) + mode_ngrp(mode)) * d * d * H * sizeof(float2);
     const size_t budget = 64ull << 20;
     int b = (int)std::max<size_t>(1, budget / per);
-    return std::min(b, 64);
+    return std::min(b, 2048);
 }
 
 // Shared-memory and thread-count plan of the three passes for side d.
@@ -298,7 +258,22 @@ static int search_impl(const void *spectra, const double *data, const float *vec
         cudaEventRecord(tm->ev[slot][pass][edge], st);
         if (edge == 1) tm->used[slot][pass] = true;
     };
-    for (int r0 = 0; r0 < nrot; r0 += batch) {
+    // fused single-kernel search where it is compiled for (mode, side)
+    bool fused = false;
+    if (want_path == 2 || want_path < 0) {
+        int frc = VESPER_OK;
+        mark(0, 0);
+        fused = vesper_fused_search(mode, dim, Src{q4, p4, data, dim}, rotmats, spectra, nrot, nscore, keys, st,
+                                    &frc) != 0;
+        if (fused && frc) return frc;
+        if (fused) {
+            mark(0, 1);
+            slot = (slot + 1) % kRing;
+        }
+    }
+    if (want_path == 2 && !fused)
+        return fail(VESPER_ERR_UNSUPPORTED, "no fused search compiled for mode %d, side %d", mode, dim);
+    for (int r0 = 0; !fused && r0 < nrot; r0 += batch) {
         const int nb = std::min(batch, nrot - r0);
         pa.r0 = r0;
         pc.r0 = r0;
@@ -391,11 +366,35 @@ extern "C" int vesper_search_profile(const void *spectra, const double *data, co
     const int rc = search_impl(spectra, data, vec, probs, dim, mode, ave, rotmats, nrot, mix, scores_out, lin_out,
                                batch, workspace, workspace_bytes, stream, &tm, opts);
     for (int p = 0; p < 4; ++p) pass_ms[p] = tm.ms[p];
+    int path = 0, launches = 0;
+    vesper_search_plan(dim, mode, batch, nrot, opts, &path, &launches);
     if (batch <= 0) batch = default_batch(dim, mode);
     const int nb = nrot > 0 ? (nrot + batch - 1) / batch : 0;
-    pass_launches[0] = pass_launches[1] = pass_launches[2] = nb;
+    pass_launches[0] = path == 2 ? (nrot > 0) : nb;
+    pass_launches[1] = pass_launches[2] = path == 2 ? 0 : nb;
     pass_launches[3] = nrot > 0 ? 1 : 0;
     return rc;
+}
+
+extern "C" int vesper_search_plan(int dim, int mode, int batch, int nrot, const int *opts, int *path_out,
+                                  int *launches_out) {
+    if (!path_out || !launches_out) return fail(VESPER_ERR_INVALID, "vesper_search_plan: NULL output");
+    FftPlan P;
+    int rc = check_dim(dim, mode, &P);
+    if (rc) return rc;
+    const int want = opts ? opts[0] : -1;
+    int path = 0;
+    if ((want == 2 || want < 0) && vesper_fused_search(mode, dim, Src{}, nullptr, nullptr, 0, 1, nullptr, nullptr,
+                                                       nullptr))
+        path = 2;
+    else if (want != 0 && want != 2 && find_reg(mode, dim))
+        path = 1;
+    if (want == 2 && path != 2) return fail(VESPER_ERR_UNSUPPORTED, "no fused search for mode %d, side %d", mode, dim);
+    if (batch <= 0) batch = default_batch(dim, mode);
+    const int nb = nrot > 0 ? (nrot + batch - 1) / batch : 0;
+    *path_out = path;
+    *launches_out = nrot > 0 ? 2 + (path == 2 ? 1 : 3 * nb) : 0;   // pack + passes + decode
+    return VESPER_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -409,6 +409,19 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
     return scores, lin
 
 
+def search_plan(dim, mode, batch=0, nrot=1, opts=None, dev=None):
+    """vesper_search_plan: (kernel family 0 radix / 1 register / 2 fused,
+    kernel launches of one search call)."""
+    dev = dev or default_device()
+    code = mode if isinstance(mode, int) else MODE_CODES[mode]
+    path = ctypes.c_int(0)
+    nl = ctypes.c_int(0)
+    copts = (ctypes.c_int * 3)(*[int(v) for v in opts]) if opts is not None else None
+    _native.check(dev.lib.vesper_search_plan(int(dim), code, int(batch), int(nrot), copts, ctypes.byref(path),
+                                             ctypes.byref(nl)))
+    return path.value, nl.value
+
+
 def topn_device(scores, topn, column=0, dev=None):
     """Stable top-N indices of scores[:, column] (int32 CUDA tensor, -1 padded)."""
     dev = dev or default_device()
