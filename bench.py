@@ -1,21 +1,30 @@
 """Benchmark: map-pair alignments per second on GB300.
 
-One step = one full alignment of a map pair with ``main.py orig`` semantics
-(threshold + grid sizing, fastVEC of both maps, target spectra, search over
-every rotation of the angle grid, top-N, +-5 degree refinement, rotated top-N
-models and their float64 scores) on seeded synthetic maps with the shapes of
-the workload named below.
+One alignment = the work of ``main.py orig`` on one map pair (threshold and
+grid sizing, fastVEC of both maps, target spectra, the rotational search,
+top-N, the +-5 degree refinement, the rotated top-N models and their float64
+scores), on seeded synthetic maps.
+
+Default workload ``prop128_s3_a10``: 128^3 / 64^3 blob-map pairs (the
+128^3/64^3 generator) at s = 3, A = 10 (24624 rotations), each aligned with the
+learned rotation proposal (the committed network ranks the grid, the exact
+search correlates the best 5%, the exhaustive search is the fallback).  A
+step aligns a batch of held-out pairs (seeds outside the training range).
+The same pairs are also aligned with the exhaustive search: the line reports
+both rates and the fraction of pairs whose top-1 rotation the two forms
+agree on.  ``--workload pair200_s2_a10``: one 200^3 / 100^3 pair per step,
+exhaustive search (no network).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 ``value``: device-resident maps, K steps timed with CUDA events between a
 barrier + synchronize on both sides, whole-job alignments/s (max over ranks).
-``e2e``: the same step through ``Aligner.align_host`` with the maps copied
+``e2e``: the same steps through ``Aligner.align_host`` with the maps copied
 from pinned host memory every step and the results read back.
 ``--impl reference``: the reference algorithm's CPU path on this host's cores
 (the oracle restatement: C fastVEC with OpenMP, numpy/scipy FFT search with
-every core), timed on a bounded sample of the same workload and scaled to a
-full alignment.
+every core), exhaustive like the reference, timed on a bounded sample of the
+same workload and scaled to a full alignment.
 """
 from __future__ import annotations
 
@@ -32,9 +41,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = "pair200_s2_a10"
+WORKLOAD = "prop128_s3_a10"
 METRIC = "map-pair alignments/s: learned-proposal vs exhaustive on GPU at ≥99% top-1 match"
 UNIT = "alignments/s"
+HELD_OUT_SEED0 = 30_000_000     # training used seeds [0, 20000)
 
 
 def parse():
@@ -43,7 +53,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--workload", default=WORKLOAD, choices=["prop128_s3_a10", "pair200_s2_a10"])
+    ap.add_argument("--pairs", type=int, default=16, help="pairs per step (prop128_s3_a10)")
     ap.add_argument("--mode", default="V", choices=list("VOCPL"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=0)
@@ -134,11 +145,28 @@ def pass_model(dim, mode):
     }
 
 
+def workload_pairs(args, rank, dev):
+    """Device maps, pinned host copies and origins of the step's pairs."""
+    import torch
+    from vesper_python_gb300 import proposal, synth
+    pairs = []
+    if args.workload == "prop128_s3_a10":
+        for i in range(args.pairs):
+            m1, m2, o1, o2 = proposal.blob_pair_torch(HELD_OUT_SEED0 + rank * args.pairs + i, device=dev.device)
+            pairs.append((m1, m2, m1.cpu().pin_memory(), m2.cpu().pin_memory(), o1, o2, 1.0))
+    else:
+        pr = synth.workload_pair(args.workload, seed=rank)   # weak scaling: one pair per rank
+        h1 = torch.from_numpy(pr.map1).pin_memory()
+        h2 = torch.from_numpy(pr.map2).pin_memory()
+        pairs.append((dev.to_dev(pr.map1), dev.to_dev(pr.map2), h1, h2, pr.orig1, pr.orig2, pr.width))
+    return pairs
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
 
-    from vesper_python_gb300 import align, synth
+    from vesper_python_gb300 import align, proposal, synth
     from vesper_python_gb300 import vesper as vg
 
     rank, world, local = dist_env()
@@ -147,14 +175,17 @@ def run_gb300(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     w = synth.WORKLOADS[args.workload]
     mode = {"V": "VecProduct", "O": "Overlap", "C": "CC", "P": "PCC", "L": "Laplacian"}[args.mode]
-    p = align.AlignParams(t=w["t"], T=w["T"], g=w["g"], s=w["s"], A=w["A"], N=w["N"], mode=mode, batch=args.batch)
-    pair = synth.workload_pair(args.workload, seed=rank)   # weak scaling: one pair per rank
     dev = vg.Device(f"cuda:{local}")
+    use_prop = args.workload == "prop128_s3_a10"
+    if use_prop and mode != "VecProduct":
+        raise SystemExit("the learned proposal workload runs in mode V")
+    net = proposal.load_weights(dev)[0] if use_prop else None
+    p = align.AlignParams(t=w["t"], T=w["T"], g=w["g"], s=w["s"], A=w["A"], N=w["N"], mode=mode, batch=args.batch,
+                          proposal=net)
+    p_exh = align.AlignParams(t=w["t"], T=w["T"], g=w["g"], s=w["s"], A=w["A"], N=w["N"], mode=mode,
+                              batch=args.batch)
+    pairs = workload_pairs(args, rank, dev)
     al = align.Aligner(dev)
-    src1 = dev.to_dev(pair.map1)
-    src2 = dev.to_dev(pair.map2)
-    h1 = torch.from_numpy(pair.map1).pin_memory()
-    h2 = torch.from_numpy(pair.map2).pin_memory()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev.device)   # > 129 MB L2
 
     def barrier():
@@ -169,64 +200,103 @@ def run_gb300(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    for _ in range(args.warmup):
-        res = al.align_device(src1, src2, pair.width, pair.width, pair.orig1, pair.orig2, p)
-    barrier()
-    # ---- timed region: device-resident inputs --------------------------------
-    clk = ClockSampler(local)
-    clk.start()
-    launches = 0
-    barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
+    def step(params):
         flush.zero_()
-        res = al.align_device(src1, src2, pair.width, pair.width, pair.orig1, pair.orig2, p)
-        launches += al.launches
-    e1.record()
-    barrier()
-    clocks = clk.stop()
-    ms = maxr(e0.elapsed_time(e1))
-    value = world * args.steps / (ms / 1e3)
-    # ---- per-pass device time of the search, one more step with events around
-    # every search launch (kept out of the timed region: the events cost ~10%)
+        out, nl = [], 0
+        for (m1, m2, _, _, o1, o2, wd) in pairs:
+            out.append(al.align_device(m1, m2, wd, wd, o1, o2, params))
+            nl += al.launches
+        return out, nl
+
+    def timed(params):
+        for _ in range(args.warmup):
+            step(params)
+        barrier()
+        clk = ClockSampler(local)
+        clk.start()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        launches = 0
+        e0.record()
+        for _ in range(args.steps):
+            res, nl = step(params)
+            launches += nl
+        e1.record()
+        barrier()
+        return maxr(e0.elapsed_time(e1)), res, launches, clk.stop()
+
+    ms, res, launches, clocks = timed(p)
+    npairs = len(pairs)
+    value = world * npairs * args.steps / (ms / 1e3)
+    fallbacks = 0
+    if use_prop:
+        # fallbacks in one step of the proposal form
+        for (m1, m2, _, _, o1, o2, wd) in pairs:
+            al.align_device(m1, m2, wd, wd, o1, o2, p)
+            fallbacks += int(bool(al.proposal_info and al.proposal_info["fallback"]))
+    # ---- per-stage and per-pass device time: one more step with events ------
     prof = {}
+    stages = {}
     al.profile = prof
-    flush.zero_()
-    al.align_device(src1, src2, pair.width, pair.width, pair.orig1, pair.orig2, p)
+    al.stages = stages
+    step(p)
     barrier()
     al.profile = None
+    al.stages = None
     # ---- end to end: host maps copied in every step -------------------------
-    for _ in range(1):
-        al.align_host(None, None, pair.width, pair.width, pair.orig1, pair.orig2, p, pinned=(h1, h2))
+    def host_step(params):
+        flush.zero_()
+        d2h = 0
+        for (_, _, h1, h2, o1, o2, wd) in pairs:
+            al.align_host(None, None, wd, wd, o1, o2, params, pinned=(h1, h2))
+            d2h += al.d2h_bytes
+        return d2h
+    host_step(p)
     barrier()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record()
     d2h = 0
     for _ in range(args.steps):
-        flush.zero_()
-        al.align_host(None, None, pair.width, pair.width, pair.orig1, pair.orig2, p, pinned=(h1, h2))
-        d2h += al.d2h_bytes
+        d2h += host_step(p)
     t1.record()
     barrier()
     e2e_ms = maxr(t0.elapsed_time(t1))
-    e2e_value = world * args.steps / (e2e_ms / 1e3)
-    dim = res.dim
+    e2e_value = world * npairs * args.steps / (e2e_ms / 1e3)
+    h2d = sum(int(h1.numel() * 4 + h2.numel() * 4) for (_, _, h1, h2, _, _, _) in pairs)
+    # ---- the exhaustive form on the same pairs --------------------------------
+    exh = None
+    if use_prop:
+        ms_x, res_x, _, _ = timed(p_exh)
+        agree = sum(int(a.top[0][0] == b.top[0][0]) for a, b in zip(res, res_x))
+        agree_model = sum(int(a.models[0].angle == b.models[0].angle and
+                              abs(a.models[0].dot_score - b.models[0].dot_score) <= 1e-4 * abs(b.models[0].dot_score))
+                          for a, b in zip(res, res_x))
+        exh = {"value": round(world * npairs * args.steps / (ms_x / 1e3), 4), "unit": UNIT,
+               "ms_per_step": round(ms_x / args.steps, 3),
+               "top1_agreement": agree / npairs, "refined_model1_agreement": agree_model / npairs,
+               "proposal_speedup": round(ms_x / ms, 3), "proposal_fallbacks_per_step": fallbacks}
+    dim = res[0].dim
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
-    # ---- roofline of the dominant kernel -------------------------------------
-    pm = pass_model(dim, args.mode if args.mode != "V" else "V")
+    # ---- roofline of the dominant search pass ---------------------------------
+    pm = pass_model(dim, args.mode)
     names = ["pass_a", "pass_b", "pass_c"]
     pass_ms = prof["pass_ms"][:3]
     pass_n = prof["pass_launches"][:3]
     top = int(np.argmax(pass_ms))
-    nrot_total = len(vg.calc_angle_comb(p.A))
-    per_launch_rot = nrot_total / pass_n[top]
-    avg_s = pass_ms[top] / pass_n[top] / 1e3
+    plan_path = vg.search_plan(dim, mode, 0, 1, None, dev)[0]
+    nrot_step = None
+    if use_prop:
+        k = int(np.ceil(0.05 * len(vg.calc_angle_comb(p.A))))
+        nrot_step = npairs * (k + 10 * 27)
+    else:
+        nrot_step = npairs * (len(vg.calc_angle_comb(p.A)) + 10 * 27)
+    per_launch_rot = nrot_step / max(1, pass_n[top])
+    avg_s = pass_ms[top] / max(1, pass_n[top]) / 1e3
     peak, peak_kind = peaks()
     ach_bytes = pm[names[top]]["bytes"] * per_launch_rot / avg_s / 1e9
     ach_flop = pm[names[top]]["flop"] * per_launch_rot / avg_s / 1e12
@@ -239,30 +309,39 @@ def run_gb300(args):
             f = ln.split()
             if len(f) == 2 and not ln.startswith("#") and f[0] == names[top]:
                 traffic = int(f[1])
-    search_ms = sum(prof["pass_ms"])
+    kname = {0: "k_pass_", 1: "k_rpass_", 2: "k_fused"}[plan_path]
+    kname = kname + names[top][-1] if plan_path != 2 else kname
+    if use_prop:
+        wl = (f"{args.workload}: {npairs} pairs per step, map1 128^3 / map2 64^3 (seeded blob maps, held-out seeds), "
+              f"s=3, A=10 (24624 rotations, 5% correlated after the learned proposal, exhaustive fallback) "
+              f"+ refinement, g=16, N=10, mode V")
+        data = "synthetic (seeded 128^3 / 64^3 blob-map pairs at 1 A, generated on the GPU)"
+    else:
+        wl = (f"{args.workload}: map1 200^3, map2 100^3, s=2, A=10 (24624 rotations + refinement), g=16, N=10, "
+              f"mode {args.mode}, exhaustive search")
+        data = "synthetic (seeded blob maps, 200^3 and 100^3 at 1 A)"
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 fastVEC, target spectra, rescoring)",
-        "data": "synthetic (seeded blob maps, 200^3 and 100^3 at 1 A)",
-        "config": {"workload": f"{args.workload}: map1 200^3, map2 100^3, s=2, A=10 (24624 rotations + refinement), "
-                               f"g=16, N=10, mode {args.mode}, exhaustive search",
-                   "grid_side": dim, "rotations": len(vg.calc_angle_comb(p.A)),
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 fastVEC, target spectra, rescoring; bf16 weights)",
+        "data": data,
+        "config": {"workload": wl, "grid_side": dim, "pairs_per_step": npairs,
+                   "rotations": len(vg.calc_angle_comb(p.A)),
                    "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{world}"},
-        "e2e": {"value": round(e2e_value, 4), "unit": UNIT,
-                "h2d_bytes_per_step": int(h1.numel() * 4 + h2.numel() * 4),
+        "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": f"search {names[top]} (k_r{names[top]} register path)",
-                     "achieved": round(ach_bytes, 1),
+        "roofline": {"bound": "hbm", "kernel": f"search {names[top]} ({kname})", "achieved": round(ach_bytes, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(ach_bytes / peak, 4), "traffic": traffic,
                      "peak_source": peak_kind,
                      "fp32": {"achieved_tflops": round(ach_flop, 3), "peak_tflops": round(fp32_peak, 1),
                               "frac": round(ach_flop / fp32_peak, 4)}},
-        "search_ms_profiled_step": round(search_ms, 3),
+        "stage_ms_profiled_step": {k: round(v, 3) for k, v in stages.items()},
         "pass_ms_profiled_step": [round(x, 3) for x in prof["pass_ms"]],
         "clocks": clocks,
     }
+    if exh is not None:
+        line["exhaustive"] = exh
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, threads=1, budget_s=12.0)
     print(json.dumps(line), flush=True)
@@ -271,12 +350,16 @@ def run_gb300(args):
 
 
 def cpu_baseline(args, threads, budget_s):
-    """The reference algorithm on this host's CPU (the oracle restatement),
-    timed on a bounded sample and scaled to one full alignment."""
+    """The reference algorithm on this host's CPU (the oracle restatement,
+    exhaustive search like the reference), timed on a bounded sample and
+    scaled to one full alignment."""
     from oracle import vesper_oracle as orc
     from vesper_python_gb300 import synth
     w = synth.WORKLOADS[args.workload]
-    pair = synth.workload_pair(args.workload, seed=0)
+    if args.workload == "prop128_s3_a10":
+        pair = synth.make_pair(HELD_OUT_SEED0, w["side1"], w["nblob"], w["radius"])
+    else:
+        pair = synth.workload_pair(args.workload, seed=0)
     m1 = orc.OMap(pair.map1, 1.0, pair.orig1)
     m2 = orc.OMap(pair.map2, 1.0, pair.orig2)
     d1, o1, c1, _ = orc.set_vox_size(m1, w["t"], w["s"])
@@ -313,8 +396,9 @@ def cpu_baseline(args, threads, budget_s):
     t_rot = (time.perf_counter() - t0) / n
     total = t_fv + R * t_rot
     return {"value": round(1.0 / total, 6), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"fastVEC on {nsamp} random voxels per map (scaled to {nvox}), search on {n} rotations "
-                      f"(scaled to {R}); {t_fv:.1f} s fastVEC + {R * t_rot:.1f} s search per alignment",
+            "sample": f"{args.workload}: fastVEC on {nsamp} random voxels per map (scaled to {nvox}), exhaustive "
+                      f"search on {n} rotations (scaled to {R}); {t_fv:.1f} s fastVEC + {R * t_rot:.1f} s search "
+                      f"per alignment",
             "seconds_per_alignment": round(total, 2)}
 
 
@@ -332,9 +416,9 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / v, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (CPU)",
-            "data": "synthetic (seeded blob maps, 200^3 and 100^3 at 1 A)",
-            "config": {"workload": f"{args.workload}: map1 200^3, map2 100^3, s=2, A=10, mode {args.mode}, "
-                                   f"CPU restatement of the reference path"},
+            "data": "synthetic (seeded blob-map pairs at 1 A)",
+            "config": {"workload": f"{args.workload}: CPU restatement of the reference path (exhaustive search), "
+                                   f"mode {args.mode}"},
             "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": cb["sample"]},
             "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

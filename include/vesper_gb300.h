@@ -221,9 +221,21 @@ int vesper_topn(const float *scores, int n, int stride, int topn, int32_t *idx_o
  *   sco_out double [d][d][d] per-voxel dot products (NULL ok)
  * ------------------------------------------------------------------------- */
 int vesper_rescore_workspace_size(int dim, size_t *bytes);
+/* With a workspace of vesper_rescore_workspace_size bytes the sums run over
+ * many blocks (chunk partials added in a fixed order); with workspace NULL
+ * they run in one block and nothing but the outputs is written. */
 int vesper_rescore(const double *tdata, const float *tvec, double tave, double tstd, double tstd_norm_ave,
                    const double *sdata, const float *svec, int dim, const int32_t *trans, double *result_out,
                    double *sco_out, void *workspace, size_t workspace_bytes, void *stream);
+/* vesper_rescore for nmodel rotated query maps at once (no counterpart in the
+ * reference: its loop calls get_score per model): sdata [nmodel][d^3],
+ * svec [nmodel][d^3][3], trans_dev DEVICE int32 [nmodel][3] already wrapped
+ * to (-d/2, d/2], result_out DEVICE double [nmodel][8].  Four launches for all
+ * models. */
+int vesper_rescore_batch_workspace_size(int dim, int nmodel, size_t *bytes);
+int vesper_rescore_batch(const double *tdata, const float *tvec, double tave, double tstd, double tstd_norm_ave,
+                         const double *sdata, const float *svec, int dim, const int32_t *trans_dev, int nmodel,
+                         double *result_out, void *workspace, size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Learned rotation proposal (no counterpart in the reference): a 3-D
@@ -237,8 +249,10 @@ int vesper_rescore(const double *tdata, const float *tvec, double tave, double t
  * the channels vx, vy, vz and (data != 0) of a fastVEC result averaged over
  * pool^3 blocks (clipped at the grid edge). */
 int vesper_prop_field(const double *data, const float *vec, int d, int pool, float *out, void *stream);
+/* One layer over nmap maps stacked in memory: in [nmap][cin][d^3] ->
+ * out [nmap][cout][d^3] (ReLU when relu != 0). */
 int vesper_prop_conv_fwd(const float *in, int cin, const void *W, const float *bias, int cout, int d, int relu,
-                         float *out, void *stream);
+                         int nmap, float *out, void *stream);
 /* Backward of one layer: din (NULL for the first layer) = input gradient;
  * dW, db ACCUMULATE (+=).  out is the layer's forward output (ReLU mask). */
 int vesper_prop_conv_bwd(const float *dout, const float *out, int relu, const float *in, const void *W, int cin,
@@ -247,21 +261,28 @@ int vesper_prop_conv_bwd(const float *dout, const float *out, int relu, const fl
  * nearest-voxel rotation gather (every in-bounds voxel accepted). */
 int vesper_prop_score(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
                       float *scores, void *stream);
+/* Channel-major [nmap][K][d^3] -> voxel-major [nmap][d^3][K]. */
+int vesper_prop_vmajor(const float *in, int K, int d, int nmap, float *out, void *stream);
+/* vesper_prop_score on voxel-major features ([d^3][K], K a multiple of 4,
+ * at most 32, 16-byte aligned): the inference form. */
+int vesper_prop_score_vm(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
+                         float *scores, void *stream);
 int vesper_prop_score_bwd_workspace(int K, int d, size_t *bytes);
 /* Gradients of sum_r gscores[r] * scores[r]; gET, gEQ ACCUMULATE (+=). */
 int vesper_prop_score_bwd(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
                           const float *gscores, float *gET, float *gEQ, void *workspace, size_t workspace_bytes,
                           void *stream);
-/* p = softmax(scores / tau): loss += -sum target log p (DEVICE float[1]),
- * gscores = (p - target) / tau. */
+/* u = scores standardised over the n rotations (mean 0, population std 1),
+ * p = softmax(u / tau): loss += -sum target log p (DEVICE float[1]);
+ * gscores = dloss/dscores through the standardisation. */
 int vesper_prop_softmax_ce(const float *scores, const float *target, int n, float tau, float *loss, float *gscores,
                            void *stream);
 /* Adam step on float32 master weights (gradient scaled by gscale), refreshing
  * the bfloat16 copy wbf16 when non-NULL. */
 int vesper_prop_adam(float *w, float *m, float *v, const float *g, int n, float lr, float b1, float b2, float eps,
                      int step, float gscale, void *wbf16, void *stream);
-/* idx_out int32[k]: indices of the k largest scores (ties to the lower index),
- * those above the k-th value first, each group in index order. */
+/* idx_out int32[k]: indices of the k largest scores (ties to the lower
+ * index), in ascending index order. */
 int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void *stream);
 
 #ifdef __cplusplus

@@ -8,6 +8,7 @@ import os
 import re
 
 import numpy as np
+import torch
 import pytest
 
 from oracle import vesper_oracle as orc
@@ -46,6 +47,38 @@ def test_rescore_matches_oracle_get_score(dev, trans):
     # the reference's per-voxel dot products are float32; ours are float64
     assert abs(sr.score - score) <= 1e-5 * max(1.0, abs(score))
     assert np.allclose(sr.sco_arr, sco, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("d", [13, 32, 75])
+def test_rescore_batch_matches_oracle_get_score(dev, d):
+    """vesper_rescore_batch (many blocks, several models, device
+    translations) against the oracle's get_score for each model."""
+    import ctypes
+    from vesper_python_gb300 import _native
+    rng = np.random.default_rng(d)
+    tdata, tvec = _field(rng, d)
+    pos = tdata[tdata > 0]
+    tave, tstd, tpstd = np.mean(pos), np.linalg.norm(pos), np.linalg.norm(pos - np.mean(pos))
+    models = [_field(rng, d) for _ in range(3)]
+    trans = [(1, 0, d - 1), (0, 0, 0), (d // 2 + 1, 2, 3)]
+    wrapped = np.array([[t - d if t > 0.5 * d else t for t in tr] for tr in trans], np.int32)
+    sd = dev.to_dev(np.stack([m[0] for m in models]))
+    sv = dev.to_dev(np.stack([m[1] for m in models]))
+    res = torch.empty((3, 8), dtype=torch.float64, device=dev.device)
+    nb = _native.size_query("vesper_rescore_batch_workspace_size", d, 3)
+    ws = torch.empty(nb, dtype=torch.uint8, device=dev.device)
+    td, tv, trd = dev.to_dev(tdata), dev.to_dev(tvec), dev.to_dev(wrapped)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    _native.check(dev.lib.vesper_rescore_batch(p(td), p(tv), tave, tstd, tpstd, p(sd), p(sv), d, p(trd), 3, p(res),
+                                               p(ws), nb, dev.stream))
+    r = res.cpu().numpy()
+    for k in range(3):
+        ov, nm, total, cc, pcc, score, _ = orc.get_score(tdata, tvec, tave, tstd, tpstd, models[k][0], models[k][1],
+                                                         trans[k])
+        assert (int(r[k, 0]), int(r[k, 1])) == (nm, total)
+        assert abs(r[k, 2] - cc) <= 1e-12 * max(1.0, abs(cc))
+        assert abs(r[k, 3] - pcc) <= 1e-12 * max(1.0, abs(pcc))
+        assert abs(r[k, 4] - score) <= 1e-5 * max(1.0, abs(score))
 
 
 def _model_lines(text, prefix):

@@ -156,19 +156,37 @@ def test_full_network_gradient_vs_oracle(dev):
         _close(net.gb[i].cpu().numpy(), grT[i][1] + grQ[i][1], 1e-3)
 
 
-@pytest.mark.parametrize("n,k", [(1, 1), (100, 7), (24624, 1232), (5000, 5000)])
+@pytest.mark.parametrize("n,k", [(1, 1), (100, 7), (24624, 1232), (5000, 5000), (3000, 1500), (70000, 3500)])
 def test_topk_subset(dev, n, k):
+    """k largest (ties, -0.0 == +0.0 included, to the lower index), returned in
+    ascending index order; 70000 scores exceed the shared-memory key buffer."""
     import ctypes
     from vesper_python_gb300 import _native
     rng = np.random.default_rng(n + k)
-    s = np.round(rng.normal(size=n) * 20) / 4          # many ties
+    s = np.round(rng.normal(size=n) * 20) / 4          # many ties, and both signed zeros
     st = dev.to_dev(s, torch.float32)
     idx = torch.full((k,), -1, dtype=torch.int32, device=dev.device)
     _native.check(dev.lib.vesper_topk_subset(ctypes.c_void_p(st.data_ptr()), n, k, ctypes.c_void_p(idx.data_ptr()),
                                              dev.stream))
-    got = np.sort(idx.cpu().numpy())
-    want = np.sort(np.lexsort((np.arange(n), -s.astype(np.float32)))[:k])
+    got = idx.cpu().numpy()
+    want = np.sort(np.argsort(-s.astype(np.float32), kind="stable")[:k])
     assert np.array_equal(got, want)
+
+
+def test_inference_scores_match_training_scores(dev):
+    """rotation_scores (stacked encoder pass, voxel-major float4 scoring)
+    against encode + vesper_prop_score on the same fields."""
+    net = _net(dev, seed=11)
+    rng = np.random.default_rng(12)
+    d = 9
+    fTQ = dev.to_dev(np.stack([_field(rng, d), _field(rng, d)]), torch.float32)
+    from vesper_python_gb300 import vesper as vg
+    mats = dev.to_dev(vg.rot_matrices(orc.calc_angle_comb(30.0)[::5]))
+    s_inf = net.rotation_scores(fTQ, mats).cpu().numpy()
+    aT = net.encode(fTQ[0].contiguous())
+    aQ = net.encode(fTQ[1].contiguous())
+    s_tr = net.score(aT[-1], aQ[-1], mats).cpu().numpy()
+    _close(s_inf, s_tr, 1e-5)
 
 
 def test_adam_step(dev):
@@ -218,3 +236,28 @@ def test_prop_field_pooling(dev, d, pool):
                 blk = full[X * pool:(X + 1) * pool, Y * pool:(Y + 1) * pool, Z * pool:(Z + 1) * pool]
                 want[:, X, Y, Z] = blk.reshape(-1, 4).mean(axis=0)
     np.testing.assert_allclose(f, want, rtol=1e-5, atol=1e-6)
+
+
+def test_trained_proposal_gain(dev):
+    """What the trained network (committed weights) gains: on 40 held-out
+    pairs (seeds outside the training range) its 5% subset holds the
+    exhaustive search's winner, so the proposal form returns the same top-1,
+    where the fixed rules without the network (mask overlap, unrotated field
+    correlation, random) miss it often; and it correlates 5% of the grid."""
+    P = _prop()
+    from vesper_python_gb300 import vesper as vg
+    net, meta = P.load_weights(dev)
+    assert meta["pairs"] >= 20000 and meta["s"] == 3.0
+    mats = vg.rot_matrices_device(vg.calc_angle_comb(meta["A"]), dev, key=("grid", meta["A"]))
+    maker = P.PairMaker(dev, s=meta["s"], pool=meta["pool"])
+    # warm-up pairs: first launches, autotuning of each grid side
+    P.evaluate(dev, net, list(range(20_100_000, 20_100_006)), mats, frac=0.05, maker=maker)
+    seeds = list(range(20_000_000, 20_000_040))
+    res, rows = P.evaluate(dev, net, seeds, mats, frac=0.05, maker=maker, baselines=("mask", "raw", "random"))
+    assert res["top1_agreement_subset_only"] >= 39 / 40
+    assert res["winner_in_subset_net"] >= 39 / 40
+    assert res["winner_in_subset_net"] >= res["winner_in_subset_mask"] + 0.1
+    assert res["winner_in_subset_net"] >= res["winner_in_subset_raw"] + 0.1
+    assert res["winner_in_subset_random"] <= 0.25
+    assert res["max_score_rel_err_when_agreeing"] <= 1e-6    # same kernels, same scores
+    assert res["search_speedup"] > 2.0

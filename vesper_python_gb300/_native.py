@@ -121,8 +121,12 @@ SIGNATURES = {
     "vesper_topn": [_vp, _i, _i, _i, _vp, _vp],
     "vesper_rescore_workspace_size": [_i, _psz],
     "vesper_rescore": [_vp, _vp, _d, _d, _d, _vp, _vp, _i, _vp, _vp, _vp, _vp, _sz, _vp],
+    "vesper_rescore_batch_workspace_size": [_i, _i, _psz],
+    "vesper_rescore_batch": [_vp, _vp, _d, _d, _d, _vp, _vp, _i, _vp, _i, _vp, _vp, _sz, _vp],
     "vesper_prop_field": [_vp, _vp, _i, _i, _vp, _vp],
-    "vesper_prop_conv_fwd": [_vp, _i, _vp, _vp, _i, _i, _i, _vp, _vp],
+    "vesper_prop_conv_fwd": [_vp, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp],
+    "vesper_prop_vmajor": [_vp, _i, _i, _i, _vp, _vp],
+    "vesper_prop_score_vm": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
     "vesper_prop_conv_bwd": [_vp, _vp, _i, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp],
     "vesper_prop_score": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
     "vesper_prop_score_bwd_workspace": [_i, _i, _psz],

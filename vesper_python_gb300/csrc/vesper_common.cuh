@@ -44,8 +44,10 @@ struct Carver {
 };
 
 // ---- ordering key for (score desc, index asc) ---------------------------------
+// -0.0 and +0.0 compare equal (as in numpy's argmax and sorts): both map to
+// the key of +0.0, so ties between them resolve by index like any other tie.
 __device__ __forceinline__ uint32_t float_order(float f) {
-    const uint32_t u = __float_as_uint(f);
+    const uint32_t u = f == 0.f ? 0u : __float_as_uint(f);
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 __device__ __forceinline__ float order_float(uint32_t o) {

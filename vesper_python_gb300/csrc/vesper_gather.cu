@@ -136,6 +136,179 @@ __global__ void __launch_bounds__(kRsThreads) k_rescore(const RescoreArgs a) {
     }
 }
 
+// ---- the same scores over many blocks and many models ---------------------------
+// Model m = blockIdx.y, voxel chunk b = blockIdx.x.  Phase 1 sums the search
+// map's statistics per chunk; a one-block reduction per model adds the chunks
+// in chunk order (deterministic) and derives ave2/std2; phase 2 sums the
+// centred norm and the overlap terms per chunk; a second reduction forms the
+// result.  Per-voxel arithmetic is that of k_rescore.
+constexpr int kRbThreads = 256;
+constexpr int kRbVoxPerThread = 8;
+constexpr int kRbParts = 6;   // doubles per chunk and model in the workspace
+
+struct RescoreBatchArgs {
+    const double *tdata;
+    const float *tvec;
+    double tave, tstd, tstd_norm_ave;
+    const double *sdata;   // [nmodel][vol]
+    const float *svec;     // [nmodel][vol][3]
+    int d, nmodel, nchunk;
+    const int32_t *trans;  // DEVICE [nmodel][3], already wrapped; NULL: (tx, ty, tz)
+    int tx, ty, tz;
+    double *part;          // [nmodel][nchunk][kRbParts]
+    double *stats;         // [nmodel][4]: n2, ave2, std2, nt
+    double *result;        // [nmodel][8]
+    double *sco;           // [vol] (nmodel == 1 only) or NULL
+};
+
+__device__ __forceinline__ void rb_chunk(const RescoreBatchArgs &a, size_t &lo, size_t &hi) {
+    const size_t vol = (size_t)a.d * a.d * a.d;
+    const size_t per = (size_t)kRbThreads * kRbVoxPerThread;
+    lo = (size_t)blockIdx.x * per;
+    hi = lo + per < vol ? lo + per : vol;
+}
+
+__global__ void __launch_bounds__(kRbThreads) k_rescore_p1(const RescoreBatchArgs a) {
+    __shared__ double red[33];
+    const int m = blockIdx.y;
+    const size_t vol = (size_t)a.d * a.d * a.d;
+    const double *sd = a.sdata + (size_t)m * vol;
+    size_t lo, hi;
+    rb_chunk(a, lo, hi);
+    double n2 = 0.0, s2 = 0.0, q2 = 0.0, nt = 0.0;
+    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const double v = sd[i];
+        if (v > 0) {
+            n2 += 1.0;
+            s2 += v;
+            q2 += v * v;
+        }
+        if (a.tdata[i] != 0.0) nt += 1.0;
+    }
+    n2 = block_sum(n2, red);
+    s2 = block_sum(s2, red);
+    q2 = block_sum(q2, red);
+    nt = block_sum(nt, red);
+    if (threadIdx.x == 0) {
+        double *p = a.part + ((size_t)m * a.nchunk + blockIdx.x) * kRbParts;
+        p[0] = n2;
+        p[1] = s2;
+        p[2] = q2;
+        p[3] = nt;
+    }
+}
+
+__global__ void k_rescore_r1(const RescoreBatchArgs a) {
+    const int m = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    double n2 = 0.0, s2 = 0.0, q2 = 0.0, nt = 0.0;
+    for (int b = 0; b < a.nchunk; ++b) {
+        const double *p = a.part + ((size_t)m * a.nchunk + b) * kRbParts;
+        n2 += p[0];
+        s2 += p[1];
+        q2 += p[2];
+        nt += p[3];
+    }
+    double *st = a.stats + (size_t)m * 4;
+    st[0] = n2;
+    st[1] = s2 / n2;
+    st[2] = sqrt(q2);
+    st[3] = nt;
+}
+
+__global__ void __launch_bounds__(kRbThreads) k_rescore_p2(const RescoreBatchArgs a) {
+    __shared__ double red[33];
+    const int m = blockIdx.y, d = a.d;
+    const size_t vol = (size_t)d * d * d;
+    const double *sd = a.sdata + (size_t)m * vol;
+    const float *sv = a.svec + (size_t)m * vol * 3;
+    const double ave2 = a.stats[(size_t)m * 4 + 1];
+    const int tx = a.trans ? a.trans[3 * m] : a.tx, ty = a.trans ? a.trans[3 * m + 1] : a.ty,
+              tz = a.trans ? a.trans[3 * m + 2] : a.tz;
+    size_t lo, hi;
+    rb_chunk(a, lo, hi);
+    double p2 = 0.0;
+    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const double v = sd[i];
+        if (v > 0) p2 += (v - ave2) * (v - ave2);
+    }
+    double cc = 0.0, pcc = 0.0, nm = 0.0, extra = 0.0, score = 0.0;
+    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const int z = (int)(i % d), y = (int)((i / d) % d), x = (int)(i / ((size_t)d * d));
+        const int sx = x + tx, sy = y + ty, sz = z + tz;
+        if (sx < 0 || sy < 0 || sz < 0 || sx >= d || sy >= d || sz >= d) continue;
+        const size_t j = ((size_t)sx * d + sy) * d + sz;
+        const double t = a.tdata[i], s = sd[j];
+        const double d1 = t <= 0 ? 0.0 : t;
+        const double d2 = s <= 0 ? 0.0 : d1;   // the reference's d2 = where(d2 <= 0, 0, d1)
+        const double pd1 = d1 <= 0 ? 0.0 : d1 - a.tave;
+        const double pd2 = d2 <= 0 ? 0.0 : d2 - ave2;
+        cc += d1 * d2;
+        pcc += pd1 * pd2;
+        if (t > 0 && s > 0) nm += 1.0;
+        if (t == 0 && s > 0) extra += 1.0;
+        const double dot = (double)a.tvec[3 * i] * (double)sv[3 * j] + (double)a.tvec[3 * i + 1] * (double)sv[3 * j + 1] +
+                           (double)a.tvec[3 * i + 2] * (double)sv[3 * j + 2];
+        score += dot;
+        if (a.sco) a.sco[j] = dot;
+    }
+    p2 = block_sum(p2, red);
+    cc = block_sum(cc, red);
+    pcc = block_sum(pcc, red);
+    nm = block_sum(nm, red);
+    extra = block_sum(extra, red);
+    score = block_sum(score, red);
+    if (threadIdx.x == 0) {
+        double *p = a.part + ((size_t)m * a.nchunk + blockIdx.x) * kRbParts;
+        p[0] = p2;
+        p[1] = cc;
+        p[2] = pcc;
+        p[3] = nm;
+        p[4] = extra;
+        p[5] = score;
+    }
+}
+
+__global__ void k_rescore_r2(const RescoreBatchArgs a) {
+    const int m = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    double acc[kRbParts] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < a.nchunk; ++b) {
+        const double *p = a.part + ((size_t)m * a.nchunk + b) * kRbParts;
+        for (int k = 0; k < kRbParts; ++k) acc[k] += p[k];
+    }
+    const double *st = a.stats + (size_t)m * 4;
+    const double pstd2 = sqrt(acc[0]);
+    double *r = a.result + (size_t)m * 8;
+    r[0] = acc[3];
+    r[1] = st[3] + acc[4];
+    r[2] = acc[1] / (a.tstd * st[2]);
+    r[3] = acc[2] / (a.tstd_norm_ave * pstd2);
+    r[4] = acc[5];
+    r[5] = st[1];
+    r[6] = st[2];
+    r[7] = pstd2;
+}
+
+static size_t rescore_chunks(int dim) {
+    const size_t vol = (size_t)dim * dim * dim;
+    const size_t per = (size_t)kRbThreads * kRbVoxPerThread;
+    return (vol + per - 1) / per;
+}
+
+static int launch_rescore_batch(RescoreBatchArgs a, cudaStream_t st) {
+    const dim3 g((unsigned)a.nchunk, (unsigned)a.nmodel);
+    k_rescore_p1<<<g, kRbThreads, 0, st>>>(a);
+    VG_CHECK_LAUNCH("k_rescore_p1");
+    k_rescore_r1<<<a.nmodel, 32, 0, st>>>(a);
+    VG_CHECK_LAUNCH("k_rescore_r1");
+    k_rescore_p2<<<g, kRbThreads, 0, st>>>(a);
+    VG_CHECK_LAUNCH("k_rescore_p2");
+    k_rescore_r2<<<a.nmodel, 32, 0, st>>>(a);
+    VG_CHECK_LAUNCH("k_rescore_r2");
+    return VESPER_OK;
+}
+
 __global__ void k_zero_f64(double *p, size_t n) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = 0.0;
@@ -159,19 +332,41 @@ extern "C" int vesper_rot_gather(const double *data, const float *vec, const flo
     return VESPER_OK;
 }
 
-extern "C" int vesper_rescore_workspace_size(int dim, size_t *bytes) {
+extern "C" int vesper_rescore_batch_workspace_size(int dim, int nmodel, size_t *bytes) {
     if (!bytes) return fail(VESPER_ERR_INVALID, "bytes is NULL");
-    (void)dim;
-    *bytes = 0;
+    if (dim < 1 || nmodel < 0) return fail(VESPER_ERR_INVALID, "vesper_rescore_batch_workspace_size: bad sizes");
+    *bytes = ((size_t)nmodel * rescore_chunks(dim) * kRbParts + (size_t)nmodel * 4) * sizeof(double) + 256;
     return VESPER_OK;
+}
+
+extern "C" int vesper_rescore_workspace_size(int dim, size_t *bytes) {
+    return vesper_rescore_batch_workspace_size(dim, 1, bytes);
+}
+
+extern "C" int vesper_rescore_batch(const double *tdata, const float *tvec, double tave, double tstd,
+                                    double tstd_norm_ave, const double *sdata, const float *svec, int dim,
+                                    const int32_t *trans_dev, int nmodel, double *result_out, void *workspace,
+                                    size_t workspace_bytes, void *stream) {
+    if (!tdata || !tvec || !sdata || !svec || !trans_dev || !result_out)
+        return fail(VESPER_ERR_INVALID, "vesper_rescore_batch: missing pointer");
+    if (dim < 1 || nmodel < 0 || nmodel > 65535) return fail(VESPER_ERR_INVALID, "vesper_rescore_batch: bad sizes");
+    if (nmodel == 0) return VESPER_OK;
+    size_t need = 0;
+    vesper_rescore_batch_workspace_size(dim, nmodel, &need);
+    if (!workspace || workspace_bytes < need) return fail(VESPER_ERR_WORKSPACE, "vesper_rescore_batch: workspace");
+    const int nchunk = (int)rescore_chunks(dim);
+    Carver cv(workspace, workspace_bytes);
+    double *part = cv.take<double>((size_t)nmodel * nchunk * kRbParts);
+    double *stats = cv.take<double>((size_t)nmodel * 4);
+    RescoreBatchArgs a{tdata, tvec, tave, tstd, tstd_norm_ave, sdata, svec, dim, nmodel, nchunk, trans_dev,
+                       0, 0, 0, part, stats, result_out, nullptr};
+    return launch_rescore_batch(a, (cudaStream_t)stream);
 }
 
 extern "C" int vesper_rescore(const double *tdata, const float *tvec, double tave, double tstd, double tstd_norm_ave,
                               const double *sdata, const float *svec, int dim, const int32_t *trans,
                               double *result_out, double *sco_out, void *workspace, size_t workspace_bytes,
                               void *stream) {
-    (void)workspace;
-    (void)workspace_bytes;
     if (!tdata || !tvec || !sdata || !svec || !trans || !result_out)
         return fail(VESPER_ERR_INVALID, "vesper_rescore: missing pointer");
     if (dim < 1) return fail(VESPER_ERR_INVALID, "vesper_rescore: bad dim");
@@ -187,6 +382,19 @@ extern "C" int vesper_rescore(const double *tdata, const float *tvec, double tav
         k_zero_f64<<<(unsigned)((vol + 255) / 256), 256, 0, st>>>(sco_out, vol);
         VG_CHECK_LAUNCH("k_zero_f64");
     }
+    size_t need = 0;
+    vesper_rescore_workspace_size(dim, &need);
+    if (workspace && workspace_bytes >= need) {
+        // many blocks: chunk partial sums in the workspace
+        const int nchunk = (int)rescore_chunks(dim);
+        Carver cv(workspace, workspace_bytes);
+        double *part = cv.take<double>((size_t)nchunk * kRbParts);
+        double *stats = cv.take<double>(4);
+        RescoreBatchArgs a{tdata, tvec, tave, tstd, tstd_norm_ave, sdata, svec, dim, 1, nchunk, nullptr,
+                           t[0], t[1], t[2], part, stats, result_out, sco_out};
+        return launch_rescore_batch(a, st);
+    }
+    // no workspace: one block
     RescoreArgs a{tdata, tvec, tave, tstd, tstd_norm_ave, sdata, svec, dim, t[0], t[1], t[2], result_out, sco_out};
     k_rescore<<<1, kRsThreads, 0, st>>>(a);
     VG_CHECK_LAUNCH("k_rescore");

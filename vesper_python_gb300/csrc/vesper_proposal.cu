@@ -27,6 +27,8 @@ __global__ void k_conv_fwd(const float *in, int cin, const __nv_bfloat16 *W, con
     const int n = d * d * d;
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     const int co = blockIdx.y;
+    in += (size_t)blockIdx.z * cin * n;     // map blockIdx.z of a stack
+    out += (size_t)blockIdx.z * cout * n;
     if (v >= n) return;
     const int x = v / (d * d), y = (v / d) % d, z = v % d;
     float acc = bias ? bias[co] : 0.f;
@@ -172,6 +174,50 @@ __global__ void k_prop_score(const float *ET, const float *EQ, int K, int d, con
     }
 }
 
+// [nmap][K][n] -> [nmap][n][K]
+__global__ void k_vmajor(const float *in, int K, int n, float *out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t per = (size_t)K * n;
+    if (i >= per) return;
+    const size_t m = blockIdx.y;
+    const int v = (int)(i / K), k = (int)(i % K);
+    out[m * per + i] = in[m * per + (size_t)k * n + v];
+}
+
+// The same scores from voxel-major features (K a multiple of 4): one voxel's
+// K channels are K/4 float4 loads, so the gathered query voxel costs whole
+// 32-byte sectors instead of K scattered words.
+template <int K4>
+__global__ void k_prop_score_vm(const float4 *ET, const float4 *EQ, int d, const float *rotmats, float *scores) {
+    __shared__ float F[9];
+    __shared__ float red[32];
+    const int r = blockIdx.x;
+    if (threadIdx.x < 9) F[threadIdx.x] = rotmats[(size_t)r * 9 + threadIdx.x];
+    __syncthreads();
+    const int n = d * d * d;
+    float acc = 0.f;
+    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+        const int s = prop_src(F, d, v);
+        if (s < 0) continue;
+#pragma unroll
+        for (int j = 0; j < K4; ++j) {
+            const float4 a = __ldg(ET + (size_t)v * K4 + j), b = __ldg(EQ + (size_t)s * K4 + j);
+            acc = fmaf(a.x, b.x, acc);
+            acc = fmaf(a.y, b.y, acc);
+            acc = fmaf(a.z, b.z, acc);
+            acc = fmaf(a.w, b.w, acc);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        scores[r] = t;
+    }
+}
+
 // Partial gradients of the correlation for channels [k0, k0 + kc): block b
 // takes rotations [b*chunk, (b+1)*chunk) and writes part[b][0][k][v] =
 // sum_r g_r EQ[k][src_r(v)] and part[b][1][k][s] = sum_r g_r ET[k][v] summed
@@ -299,10 +345,18 @@ __global__ void k_adam(float *w, float *m, float *v, const float *g, int n, floa
 
 // ---- top-k subset: indices of the k largest scores (ties to lower index) --------
 // One block: bisection on the order-preserving bit pattern for the k-th
-// largest value, then an ordered compaction.
-__global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int k, int32_t *idx) {
+// largest value, then an ordered compaction.  The keys sit in shared memory
+// when they fit (skeys), else they are re-read from global memory each round.
+__global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int k, int32_t *idx, int skeys) {
+    extern __shared__ uint32_t keys[];
     __shared__ unsigned int cnt;
     __shared__ int ncount[1024 / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (skeys) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = float_order(s[i]);
+        __syncthreads();
+    }
+    auto key = [&](int i) -> uint32_t { return skeys ? keys[i] : float_order(s[i]); };
     uint32_t lo = 0u, hi = 0xffffffffu;   // answer in [lo, hi]: count(key >= t) >= k
     // the interval halves every round (midpoint taken in 64 bits), so 32
     // rounds reach lo == hi; the bound is explicit all the same
@@ -311,8 +365,9 @@ __global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int
         if (threadIdx.x == 0) cnt = 0u;
         __syncthreads();
         unsigned int c = 0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) c += float_order(s[i]) >= mid;
-        atomicAdd(&cnt, c);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) c += key(i) >= mid;
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+        if (lane == 0) atomicAdd(&cnt, c);
         __syncthreads();
         if (cnt >= (unsigned)k)
             lo = mid;
@@ -325,38 +380,41 @@ __global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int
     if (threadIdx.x == 0) cnt = 0u;
     __syncthreads();
     unsigned int above = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) above += float_order(s[i]) > t;
-    atomicAdd(&cnt, above);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) above += key(i) > t;
+    for (int o = 16; o > 0; o >>= 1) above += __shfl_down_sync(0xffffffffu, above, o);
+    if (lane == 0) atomicAdd(&cnt, above);
     __syncthreads();
     const int n_above = (int)cnt;
-    // ordered compaction with a block-wide prefix over fixed-size tiles
-    int base_above = 0, base_tie = 0;
+    // one ordered compaction: every index above the threshold and the first
+    // (k - n_above) ties, in ascending index order
+    const int ties_wanted = k - n_above;
+    int base_sel = 0, base_tie = 0;
     for (int start = 0; start < n; start += blockDim.x) {
         const int i = start + threadIdx.x;
-        const uint32_t key = i < n ? float_order(s[i]) : 0u;
-        const int is_above = i < n && key > t, is_tie = i < n && key == t;
-        // warp-level ballots then a per-warp prefix
-        const unsigned ma = __ballot_sync(0xffffffffu, is_above), mt = __ballot_sync(0xffffffffu, is_tie);
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (lane == 0) ncount[warp] = (__popc(ma) << 16) | __popc(mt);
-        __syncthreads();
-        int pa = 0, pt = 0;
-        for (int w = 0; w < warp; ++w) {
-            pa += ncount[w] >> 16;
-            pt += ncount[w] & 0xffff;
-        }
+        const uint32_t kv = i < n ? key(i) : 0u;
+        const int is_above = i < n && kv > t, is_tie = i < n && kv == t;
         const unsigned lower = (1u << lane) - 1u;
-        if (is_above) idx[base_above + pa + __popc(ma & lower)] = i;
-        if (is_tie) {
-            const int pos = base_tie + pt + __popc(mt & lower);
-            if (n_above + pos < k) idx[n_above + pos] = i;
-        }
-        int ta = 0, tt = 0;
+        // tie positions first (warp ballot, then a prefix over the warps)
+        const unsigned mt = __ballot_sync(0xffffffffu, is_tie);
+        if (lane == 0) ncount[warp] = __popc(mt);
+        __syncthreads();
+        int pt = 0, tt = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-            ta += ncount[w] >> 16;
-            tt += ncount[w] & 0xffff;
+            if (w < warp) pt += ncount[w];
+            tt += ncount[w];
         }
-        base_above += ta;
+        const int sel = is_above || (is_tie && base_tie + pt + __popc(mt & lower) < ties_wanted);
+        __syncthreads();
+        const unsigned ms = __ballot_sync(0xffffffffu, sel);
+        if (lane == 0) ncount[warp] = __popc(ms);
+        __syncthreads();
+        int ps = 0, ts = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            if (w < warp) ps += ncount[w];
+            ts += ncount[w];
+        }
+        if (sel) idx[base_sel + ps + __popc(ms & lower)] = i;
+        base_sel += ts;
         base_tie += tt;
         __syncthreads();
     }
@@ -376,10 +434,11 @@ extern "C" int vesper_prop_field(const double *data, const float *vec, int d, in
 }
 
 extern "C" int vesper_prop_conv_fwd(const float *in, int cin, const void *W, const float *bias, int cout, int d,
-                                    int relu, float *out, void *stream) {
-    if (!in || !W || !out || cin < 1 || cout < 1 || d < 1) return fail(VESPER_ERR_INVALID, "conv_fwd: bad args");
+                                    int relu, int nmap, float *out, void *stream) {
+    if (!in || !W || !out || cin < 1 || cout < 1 || d < 1 || nmap < 1 || nmap > 65535)
+        return fail(VESPER_ERR_INVALID, "conv_fwd: bad args");
     const int n = d * d * d;
-    k_conv_fwd<<<dim3((n + 127) / 128, cout), 128, 0, (cudaStream_t)stream>>>(
+    k_conv_fwd<<<dim3((n + 127) / 128, cout, nmap), 128, 0, (cudaStream_t)stream>>>(
         in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
     VG_CHECK_LAUNCH("k_conv_fwd");
     return VESPER_OK;
@@ -408,6 +467,33 @@ extern "C" int vesper_prop_score(const float *ET, const float *EQ, int K, int d,
     if (nrot == 0) return VESPER_OK;
     k_prop_score<<<nrot, 256, 0, (cudaStream_t)stream>>>(ET, EQ, K, d, rotmats, nrot, scores);
     VG_CHECK_LAUNCH("k_prop_score");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_vmajor(const float *in, int K, int d, int nmap, float *out, void *stream) {
+    if (!in || !out || K < 1 || d < 1 || nmap < 1 || nmap > 65535) return fail(VESPER_ERR_INVALID, "vmajor: bad args");
+    const size_t per = (size_t)K * d * d * d;
+    k_vmajor<<<dim3((unsigned)((per + 255) / 256), nmap), 256, 0, (cudaStream_t)stream>>>(in, K, d * d * d, out);
+    VG_CHECK_LAUNCH("k_vmajor");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_score_vm(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
+                                    float *scores, void *stream) {
+    if (!ET || !EQ || !rotmats || !scores || d < 1 || nrot < 0 || K < 4 || K % 4 || K > 32)
+        return fail(VESPER_ERR_INVALID, "prop_score_vm: bad args (K a multiple of 4, <= 32)");
+    if (((uintptr_t)ET | (uintptr_t)EQ) & 15) return fail(VESPER_ERR_INVALID, "prop_score_vm: 16-byte alignment");
+    if (nrot == 0) return VESPER_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const float4 *a = (const float4 *)ET, *b = (const float4 *)EQ;
+    switch (K / 4) {
+        case 1: k_prop_score_vm<1><<<nrot, 256, 0, st>>>(a, b, d, rotmats, scores); break;
+        case 2: k_prop_score_vm<2><<<nrot, 256, 0, st>>>(a, b, d, rotmats, scores); break;
+        case 4: k_prop_score_vm<4><<<nrot, 256, 0, st>>>(a, b, d, rotmats, scores); break;
+        case 8: k_prop_score_vm<8><<<nrot, 256, 0, st>>>(a, b, d, rotmats, scores); break;
+        default: return fail(VESPER_ERR_UNSUPPORTED, "prop_score_vm: K = %d", K);
+    }
+    VG_CHECK_LAUNCH("k_prop_score_vm");
     return VESPER_OK;
 }
 
@@ -468,7 +554,11 @@ extern "C" int vesper_prop_adam(float *w, float *m, float *v, const float *g, in
 
 extern "C" int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void *stream) {
     if (!scores || !idx_out || n < 1 || k < 1 || k > n) return fail(VESPER_ERR_INVALID, "topk_subset: bad args");
-    k_topk_subset<<<1, 1024, 0, (cudaStream_t)stream>>>(scores, n, k, idx_out);
+    const size_t kb = (size_t)n * sizeof(uint32_t);
+    const int skeys = kb <= (size_t)smem_limit() - 4096 ? 1 : 0;
+    const size_t sm = skeys ? kb : 0;
+    if (skeys) allow_smem(k_topk_subset, sm);
+    k_topk_subset<<<1, 1024, sm, (cudaStream_t)stream>>>(scores, n, k, idx_out, skeys);
     VG_CHECK_LAUNCH("k_topk_subset");
     return VESPER_OK;
 }

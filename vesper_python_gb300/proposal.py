@@ -38,13 +38,13 @@ def _p(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
-def map_field(data, vec, pool=1, dev=None):
+def map_field(data, vec, pool=1, dev=None, out=None):
     """4-channel network input [4][dp][dp][dp] (vx, vy, vz, mask) of a fastVEC
     result, averaged over pool^3 blocks (vesper_prop_field)."""
     dev = dev or vg.default_device()
     d = int(data.shape[0])
     dp = (d + pool - 1) // pool
-    f = torch.empty((4, dp, dp, dp), dtype=torch.float32, device=data.device)
+    f = out if out is not None else torch.empty((4, dp, dp, dp), dtype=torch.float32, device=data.device)
     _native.check(dev.lib.vesper_prop_field(_p(data), _p(vec), d, int(pool), _p(f), dev.stream))
     return f
 
@@ -88,13 +88,16 @@ class ProposalNet:
         self.step_count = int(s.get("step", 0))
 
     # ---- forward / backward ------------------------------------------------
-    def encode(self, field):
+    def encode(self, field, nmap=1):
+        """Activations of every layer; ``field`` is [4][d][d][d], or
+        [nmap][4][d][d][d] for nmap maps encoded in one launch per layer."""
         acts = [field.contiguous()]
-        d = int(field.shape[1])
+        d = int(field.shape[-1])
+        lead = (nmap,) if nmap > 1 else ()
         for i, (cin, cout) in enumerate(zip(CHANNELS[:-1], CHANNELS[1:])):
-            out = torch.empty((cout, d, d, d), dtype=torch.float32, device=self.dev.device)
+            out = torch.empty(lead + (cout, d, d, d), dtype=torch.float32, device=self.dev.device)
             _native.check(self.lib.vesper_prop_conv_fwd(_p(acts[-1]), cin, _p(self.Wbf[i]), _p(self.b[i]), cout, d,
-                                                        self.relu[i], _p(out), self.dev.stream))
+                                                        self.relu[i], nmap, _p(out), self.dev.stream))
             acts.append(out)
         return acts
 
@@ -154,16 +157,26 @@ class ProposalNet:
                                                     self.b[i].numel(), lr, b1, b2, eps, self.step_count,
                                                     1.0 / batch, None, self.dev.stream))
 
-    def propose(self, fT, fQ, mats, frac):
-        """Indices of the best ``frac`` of the rotations (int32, device)."""
-        aT = self.encode(fT)
-        aQ = self.encode(fQ)
-        s = self.score(aT[-1], aQ[-1], mats)
-        n = int(s.numel())
-        k = max(1, int(math.ceil(frac * n)))
-        idx = torch.empty(k, dtype=torch.int32, device=self.dev.device)
-        _native.check(self.lib.vesper_topk_subset(_p(s), n, k, _p(idx), self.dev.stream))
-        return idx, s
+    def rotation_scores(self, fTQ, mats):
+        """Inference: both maps' fields stacked [2][4][d][d][d] -> score of
+        every rotation (one encoder pass over the stack, voxel-major
+        features, vesper_prop_score_vm)."""
+        d = int(fTQ.shape[-1])
+        K = CHANNELS[-1]
+        feat = self.encode(fTQ, nmap=2)[-1]
+        vm = torch.empty((2, d * d * d, K), dtype=torch.float32, device=self.dev.device)
+        _native.check(self.lib.vesper_prop_vmajor(_p(feat), K, d, 2, _p(vm), self.dev.stream))
+        n = int(mats.shape[0])
+        s = torch.empty(n, dtype=torch.float32, device=self.dev.device)
+        _native.check(self.lib.vesper_prop_score_vm(_p(vm[0]), _p(vm[1]), K, d, _p(mats), n, _p(s),
+                                                    self.dev.stream))
+        return s
+
+    def propose(self, fTQ, mats, frac):
+        """Grid indices (int32, ascending) of the best ``frac`` of the
+        rotations, and the scores of all of them."""
+        s = self.rotation_scores(fTQ, mats)
+        return subset_from_scores(self.dev, s, frac), s
 
 
 def target_distribution(scores, beta):
@@ -180,7 +193,8 @@ def target_distribution(scores, beta):
 
 @dataclasses.dataclass
 class PairFields:
-    fT: torch.Tensor
+    fTQ: torch.Tensor        # [2][4][dp][dp][dp]: target then query network input
+    fT: torch.Tensor         # views of fTQ[0], fTQ[1]
     fQ: torch.Tensor
     tdata: torch.Tensor
     tvec: torch.Tensor
@@ -269,24 +283,17 @@ class PairMaker:
             no1 = c1 - 0.5 * self.s * dim
         td, _, tv = vg.fastvec_device(m1, 1.0, oo1.astype(np.float64), dim, self.s, no1, self.g, dev=self.dev)
         qd, _, qv = vg.fastvec_device(m2, 1.0, oo2.astype(np.float64), dim, self.s, no2, self.g, dev=self.dev)
-        return PairFields(map_field(td, tv, self.pool, self.dev), map_field(qd, qv, self.pool, self.dev),
-                          td, tv, qd, qv, dim)
+        dp = (dim + self.pool - 1) // self.pool
+        fTQ = torch.empty((2, 4, dp, dp, dp), dtype=torch.float32, device=self.dev.device)
+        map_field(td, tv, self.pool, self.dev, out=fTQ[0])
+        map_field(qd, qv, self.pool, self.dev, out=fTQ[1])
+        return PairFields(fTQ, fTQ[0], fTQ[1], td, tv, qd, qv, dim)
 
 
 def exhaustive_scores(dev, pf: PairFields, mats):
     spec = vg.target_spectra_device(pf.tdata, pf.tvec, "VecProduct", 0.0, dev=dev)
     sc, ln = vg.search_device(spec, pf.qdata, pf.qvec, "VecProduct", 0.0, mats, dev=dev, tuned=True)
     return spec, sc[:, 0].contiguous(), ln[:, 0].contiguous()
-
-
-def proposal_search(dev, net, pf: PairFields, mats, frac, spec=None):
-    """Best (score, rotation index) over the proposed fraction of the grid."""
-    idx, _ = net.propose(pf.fT, pf.fQ, mats, frac)
-    sub = mats.index_select(0, idx.to(torch.int64))
-    if spec is None:
-        spec = vg.target_spectra_device(pf.tdata, pf.tvec, "VecProduct", 0.0, dev=dev)
-    sc, ln = vg.search_device(spec, pf.qdata, pf.qvec, "VecProduct", 0.0, sub, dev=dev, tuned=True)
-    return idx, sc[:, 0], ln[:, 0]
 
 
 def label_pairs(dev, maker, seeds, mats, beta, cache, log=None):
@@ -405,7 +412,7 @@ class ProposalResult:
     fallback: bool
     winner_rank: int         # network rank of the subset's best rotation
     winner_z: float          # its exact score, z-scored over the subset
-    subset: np.ndarray       # the correlated rotations (grid indices, ascending)
+    subset: torch.Tensor     # the correlated rotations (grid indices, ascending; device)
     subset_top: np.ndarray   # top-N of the subset alone (before any fallback)
 
 
@@ -415,39 +422,41 @@ def _top_from(dev, sc, ln, ridx, N):
     return ridx[top], sc.cpu().numpy()[top], ln.cpu().numpy()[top]
 
 
-def search_with_proposal(dev, net, pf: PairFields, spec, mats, frac=0.05, N=10, fallback_rank=0.5,
+def search_with_proposal(dev, net, pf: PairFields, spec, mats, frac=0.05, N=10, fallback_rank=1.0,
                          fallback_z=None, scores=None):
     """Correlate the best ``frac`` of the grid by the network's ranking.  The
     whole grid is correlated instead (the fallback) when the subset's best
     rotation ranks below ``fallback_rank`` of the subset in the network's own
     order, or when its exact score stands less than ``fallback_z`` standard
-    deviations above the subset's mean (a flat landscape)."""
-    s = scores if scores is not None else net.propose(pf.fT, pf.fQ, mats, frac)[1]
-    idx = subset_from_scores(dev, s, frac)
-    k = int(idx.numel())
-    order = torch.sort(idx.to(torch.int64)).values     # grid order: ties resolve to the lower index
+    deviations above the subset's mean (a flat landscape).  One device-to-host
+    copy when there is no fallback."""
+    s = scores if scores is not None else net.rotation_scores(pf.fTQ, mats)
+    order = subset_from_scores(dev, s, frac).to(torch.int64)     # ascending grid indices
+    k = int(order.numel())
     sub = mats.index_select(0, order)
     sc, ln = vg.search_device(spec, pf.qdata, pf.qvec, "VecProduct", 0.0, sub, dev=dev, tuned=True)
     sc0, ln0 = sc[:, 0].contiguous(), ln[:, 0].contiguous()
-    top = vg.topn_device(sc0, N, dev=dev).to(torch.int64)
+    nt = min(N, k)
+    top = vg.topn_device(sc0, nt, dev=dev)[:nt].to(torch.int64)   # positions in the subset
     w = top[0]
     sv = s.index_select(0, order)
-    rank = (sv > sv[w]).sum()
-    z = (sc0[w] - sc0.mean()) / (sc0.std() + 1e-30)
-    oh = order.cpu().numpy()
-    th = top.cpu().numpy()
-    th = th[th >= 0]
-    rank, z = int(rank.item()), float(z.item())
-    stop = oh[th]
+    rank = (sv > sv[w]).sum().to(torch.float64)
+    z = ((sc0[w] - sc0.mean()) / (sc0.std() + 1e-30)).to(torch.float64)
+    packed = torch.cat([torch.stack([rank, z]), order[top].to(torch.float64), sc0[top].to(torch.float64),
+                        ln0[top].to(torch.float64)]).cpu().numpy()
+    rank, z = int(packed[0]), float(packed[1])
+    stop = packed[2:2 + nt].astype(np.int64)
+    tsc = packed[2 + nt:2 + 2 * nt].astype(np.float32)
+    tln = packed[2 + 2 * nt:].astype(np.int64)
     fb = rank > fallback_rank * k or (fallback_z is not None and z < fallback_z)
     if fb:
         fs, fl = vg.search_device(spec, pf.qdata, pf.qvec, "VecProduct", 0.0, mats, dev=dev, tuned=True)
-        t, tsc, tln = _top_from(dev, fs[:, 0], fl[:, 0], np.arange(int(mats.shape[0])), N)
-        return ProposalResult(t, tsc, tln, True, rank, z, oh, stop)
-    return ProposalResult(stop, sc0.cpu().numpy()[th], ln0.cpu().numpy()[th], False, rank, z, oh, stop)
+        t, fsc, fln = _top_from(dev, fs[:, 0], fl[:, 0], np.arange(int(mats.shape[0])), N)
+        return ProposalResult(t, fsc, fln, True, rank, z, order, stop)
+    return ProposalResult(stop, tsc, tln, False, rank, z, order, stop)
 
 
-def evaluate(dev, net, seeds, mats, frac=0.05, N=10, fallback_rank=0.5, fallback_z=None, maker=None,
+def evaluate(dev, net, seeds, mats, frac=0.05, N=10, fallback_rank=1.0, fallback_z=None, maker=None,
              baselines=(), log=None):
     """Top-1 / top-N agreement with the exhaustive search and the search-stage
     time of both forms over the given pair seeds, with per-pair diagnostics
@@ -476,7 +485,7 @@ def evaluate(dev, net, seeds, mats, frac=0.05, N=10, fallback_rank=0.5, fallback
                "top1_subset": bool(pr.subset_top[0] == win),
                "topN": len(set(pr.top.tolist()) & set(ex_top.tolist())) / max(1, len(ex_top)),
                "fallback": pr.fallback, "rank": pr.winner_rank, "z": pr.winner_z,
-               "in_subset_net": bool(win in set(pr.subset.tolist())),
+               "in_subset_net": bool(win in set(pr.subset.cpu().numpy().tolist())),
                "score_rel_err": float(abs(pr.scores[0] - ex_sc[0]) / max(abs(ex_sc[0]), 1e-30))}
         for kind in baselines:
             sub = subset_from_scores(dev, baseline_scores(dev, pf, mats, kind), frac).cpu().numpy()

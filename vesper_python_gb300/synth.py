@@ -142,6 +142,8 @@ WORKLOADS = {
                            modes=("V",)),
     "pair200_s2_a10": dict(side1=200, nblob=1500, radius=70.0, t=0.1, T=0.1, g=16.0, s=2.0, A=10.0, N=10,
                            modes=("V", "O", "C", "P", "L")),
+    "prop128_s3_a10": dict(side1=128, nblob=400, radius=40.0, t=0.1, T=0.1, g=16.0, s=3.0, A=10.0, N=10,
+                           modes=("V",)),
     "prob128_s3_a15": dict(side1=128, nblob=400, radius=40.0, t=0.1, T=0.1, g=16.0, s=3.0, A=15.0, N=10,
                            modes=("V",), alpha=0.5, prob=True, pad=64),
 }

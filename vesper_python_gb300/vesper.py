@@ -487,9 +487,10 @@ def get_score_device(target_map, sdata, svec, trans, want_arr=True, dev=None):
     res = torch.empty(8, dtype=torch.float64, device=dev.device)
     sco = torch.empty((d, d, d), dtype=torch.float64, device=dev.device) if want_arr else None
     tr = (ctypes.c_int32 * 3)(*[int(t) for t in trans])
+    ws = dev.workspace(("rescore", d), _native.size_query("vesper_rescore_workspace_size", d))
     _native.check(dev.lib.vesper_rescore(_ptr(tdata), _ptr(tvec), float(target_map.ave), float(target_map.std),
                                          float(target_map.std_norm_ave), _ptr(sdata), _ptr(svec), d, tr, _ptr(res),
-                                         _ptr(sco), None, 0, dev.stream))
+                                         _ptr(sco), _ptr(ws), ws.numel(), dev.stream))
     r = res.cpu().numpy()
     nm, total = int(r[0]), int(r[1])
     return ScoreResult(float(nm) / float(total), nm, total, float(r[2]), float(r[3]), float(r[4]),
