@@ -12,14 +12,15 @@ search correlates the best 5%, the exhaustive search is the fallback).  A
 step aligns a batch of held-out pairs (seeds outside the training range).
 The same pairs are also aligned with the exhaustive search: the line reports
 both rates and the fraction of pairs whose top-1 rotation the two forms
-agree on.  ``--workload pair200_s2_a10``: one 200^3 / 100^3 pair per step,
-exhaustive search (no network).
+agree on.  A step runs ``Aligner.align_many`` over its pairs: every stage is
+launched for all pairs before the host waits.  ``--workload pair200_s2_a10``:
+one 200^3 / 100^3 pair per step, exhaustive search (no network).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 ``value``: device-resident maps, K steps timed with CUDA events between a
 barrier + synchronize on both sides, whole-job alignments/s (max over ranks).
-``e2e``: the same steps through ``Aligner.align_host`` with the maps copied
+``e2e``: the same steps through ``Aligner.align_host_many`` with the maps copied
 from pinned host memory every step and the results read back.
 ``--impl reference``: the reference algorithm's CPU path on this host's cores
 (the oracle restatement: C fastVEC with OpenMP, numpy/scipy FFT search with
@@ -58,6 +59,8 @@ def parse():
     ap.add_argument("--mode", default="V", choices=list("VOCPL"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--no-exhaustive", action="store_true",
+                    help="skip the exhaustive form on the same pairs (profiling runs)")
     return ap.parse_args()
 
 
@@ -200,13 +203,13 @@ def run_gb300(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    dev_items = [(m1, m2, wd, wd, o1, o2) for (m1, m2, _, _, o1, o2, wd) in pairs]
+    host_items = [(h1, h2, wd, wd, o1, o2) for (_, _, h1, h2, o1, o2, wd) in pairs]
+
     def step(params):
         flush.zero_()
-        out, nl = [], 0
-        for (m1, m2, _, _, o1, o2, wd) in pairs:
-            out.append(al.align_device(m1, m2, wd, wd, o1, o2, params))
-            nl += al.launches
-        return out, nl
+        out = al.align_many(dev_items, params)
+        return out, al.launches
 
     def timed(params):
         for _ in range(args.warmup):
@@ -232,26 +235,24 @@ def run_gb300(args):
     fallbacks = 0
     if use_prop:
         # fallbacks in one step of the proposal form
-        for (m1, m2, _, _, o1, o2, wd) in pairs:
-            al.align_device(m1, m2, wd, wd, o1, o2, p)
-            fallbacks += int(bool(al.proposal_info and al.proposal_info["fallback"]))
+        al.align_many(dev_items, p)
+        fallbacks = sum(al.proposal_info["fallback"])
     # ---- per-stage and per-pass device time: one more step with events ------
-    prof = {}
     stages = {}
-    al.profile = prof
-    al.stages = stages
+    al.stages = stages       # stage boundaries only: events between stages
+    step(p)
+    barrier()
+    al.stages = None
+    prof = {}
+    al.profile = prof        # events around every search launch (slower; its own step)
     step(p)
     barrier()
     al.profile = None
-    al.stages = None
     # ---- end to end: host maps copied in every step -------------------------
     def host_step(params):
         flush.zero_()
-        d2h = 0
-        for (_, _, h1, h2, o1, o2, wd) in pairs:
-            al.align_host(None, None, wd, wd, o1, o2, params, pinned=(h1, h2))
-            d2h += al.d2h_bytes
-        return d2h
+        al.align_host_many(host_items, params)
+        return al.d2h_bytes
     host_step(p)
     barrier()
     t0 = torch.cuda.Event(enable_timing=True)
@@ -267,7 +268,7 @@ def run_gb300(args):
     h2d = sum(int(h1.numel() * 4 + h2.numel() * 4) for (_, _, h1, h2, _, _, _) in pairs)
     # ---- the exhaustive form on the same pairs --------------------------------
     exh = None
-    if use_prop:
+    if use_prop and not args.no_exhaustive:
         ms_x, res_x, _, _ = timed(p_exh)
         agree = sum(int(a.top[0][0] == b.top[0][0]) for a, b in zip(res, res_x))
         agree_model = sum(int(a.models[0].angle == b.models[0].angle and

@@ -73,6 +73,12 @@ int vesper_prepare_map(float *data, int sx, int sy, int sz, double threshold, co
  * stats_out DEVICE double[5] = {sum, count != 0, mean of > 0, L2 norm of > 0,
  * L2 norm of (> 0 values - mean)}. */
 int vesper_map_stats(const double *data, int dim, double *stats_out, void *stream);
+/* The same statistics over many blocks, with a caller workspace of
+ * vesper_map_stats_workspace_size bytes (chunk partial sums added in a fixed
+ * order).  No counterpart in the reference. */
+int vesper_map_stats_workspace_size(int dim, size_t *bytes);
+int vesper_map_stats_ws(const double *data, int dim, double *stats_out, void *workspace, size_t workspace_bytes,
+                        void *stream);
 
 /* ---------------------------------------------------------------------------
  * fastVEC: Gaussian-weighted unit-vector field of one resampled map.
@@ -267,6 +273,20 @@ int vesper_prop_vmajor(const float *in, int K, int d, int nmap, float *out, void
  * at most 32, 16-byte aligned): the inference form. */
 int vesper_prop_score_vm(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,
                          float *scores, void *stream);
+/* Inference form with float16 voxel-major features ([d^3][K] half, K a
+ * multiple of 8, at most 32, 16-byte aligned), four rotations per block,
+ * float32 accumulation; vesper_prop_vmajor_f16 writes that layout from
+ * channel-major float32 [nmap][K][d^3]. */
+int vesper_prop_vmajor_f16(const float *in, int K, int d, int nmap, void *out, void *stream);
+int vesper_prop_score_f16(const void *ET, const void *EQ, int K, int d, const float *rotmats, int nrot,
+                          float *scores, void *stream);
+/* The gather geometry of every (rotation, voxel) of a d^3 grid, d^3 <= 32767:
+ * srcmap_out int16 [nrot][d^3] (-1: none), computed once per grid and
+ * rotation set; vesper_prop_score_map scores from it (float16 voxel-major
+ * features as for vesper_prop_score_f16) without recomputing the geometry. */
+int vesper_prop_srcmap(int d, const float *rotmats, int nrot, void *srcmap_out, void *stream);
+int vesper_prop_score_map(const void *ET, const void *EQ, int K, int d, const void *srcmap, int nrot,
+                          float *scores, void *stream);
 int vesper_prop_score_bwd_workspace(int K, int d, size_t *bytes);
 /* Gradients of sum_r gscores[r] * scores[r]; gET, gEQ ACCUMULATE (+=). */
 int vesper_prop_score_bwd(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,

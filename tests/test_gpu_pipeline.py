@@ -153,3 +153,44 @@ def test_prob_pipeline_top_models(dev, golden_dir, tmp_path):
     out = buf.getvalue()
     ref = open(os.path.join(golden_dir, "prob_pair128.txt")).read()
     assert _model_lines(out, "#") == _model_lines(ref, "#")
+
+
+def test_align_many_equals_one_at_a_time(dev):
+    """A batch of uneven pairs through align_many gives, pair by pair, what
+    align_device gives for each pair alone."""
+    from vesper_python_gb300 import align, synth
+    al = align.Aligner(dev)
+    p = align.AlignParams(t=0.1, T=0.1, g=16.0, s=7.0, A=30.0, N=5, mode="VecProduct")
+    pairs = [synth.uneven_pair(i) for i in range(3)]
+    items = [(dev.to_dev(pr.map1), dev.to_dev(pr.map2), pr.width, pr.width, pr.orig1, pr.orig2) for pr in pairs]
+    many = al.align_many(items, p)
+    for it, r in zip(items, many):
+        one = al.align_device(*it, p)
+        assert one.dim == r.dim
+        assert [m.angle for m in one.models] == [m.angle for m in r.models]
+        assert [m.vec_trans for m in one.models] == [m.vec_trans for m in r.models]
+        assert [m.dot_score for m in one.models] == [m.dot_score for m in r.models]
+        assert one.top == r.top
+
+
+@pytest.mark.parametrize("d", [13, 30, 75])
+def test_map_stats_many_blocks(dev, d):
+    """vesper_map_stats_ws (many blocks) against numpy and the one-block form."""
+    import ctypes
+    from vesper_python_gb300 import _native
+    rng = np.random.default_rng(d)
+    data = rng.uniform(-0.5, 2.0, size=(d, d, d))
+    data[rng.random((d, d, d)) < 0.3] = 0.0
+    t = dev.to_dev(data)
+    a = torch.empty(5, dtype=torch.float64, device=dev.device)
+    b = torch.empty(5, dtype=torch.float64, device=dev.device)
+    nb = _native.size_query("vesper_map_stats_workspace_size", d)
+    ws = torch.empty(nb, dtype=torch.uint8, device=dev.device)
+    p = lambda x: ctypes.c_void_p(x.data_ptr())
+    _native.check(dev.lib.vesper_map_stats(p(t), d, p(a), dev.stream))
+    _native.check(dev.lib.vesper_map_stats_ws(p(t), d, p(b), p(ws), nb, dev.stream))
+    pos = data[data > 0]
+    want = np.array([data.sum(), np.count_nonzero(data), pos.mean(), np.linalg.norm(pos),
+                     np.linalg.norm(pos - pos.mean())])
+    np.testing.assert_allclose(a.cpu().numpy(), want, rtol=1e-12)
+    np.testing.assert_allclose(b.cpu().numpy(), want, rtol=1e-12)

@@ -182,11 +182,13 @@ def test_inference_scores_match_training_scores(dev):
     fTQ = dev.to_dev(np.stack([_field(rng, d), _field(rng, d)]), torch.float32)
     from vesper_python_gb300 import vesper as vg
     mats = dev.to_dev(vg.rot_matrices(orc.calc_angle_comb(30.0)[::5]))
-    s_inf = net.rotation_scores(fTQ, mats).cpu().numpy()
+    s_inf = net.rotation_scores(fTQ, mats, half=False).cpu().numpy()
+    s_half = net.rotation_scores(fTQ, mats, half=True).cpu().numpy()
     aT = net.encode(fTQ[0].contiguous())
     aQ = net.encode(fTQ[1].contiguous())
     s_tr = net.score(aT[-1], aQ[-1], mats).cpu().numpy()
     _close(s_inf, s_tr, 1e-5)
+    _close(s_half, s_tr, 2e-3)     # float16 features, float32 sums
 
 
 def test_adam_step(dev):
@@ -261,3 +263,29 @@ def test_trained_proposal_gain(dev):
     assert res["winner_in_subset_random"] <= 0.25
     assert res["max_score_rel_err_when_agreeing"] <= 1e-6    # same kernels, same scores
     assert res["search_speedup"] > 2.0
+
+
+@pytest.mark.parametrize("d", [7, 8, 15])
+def test_srcmap_scores_match_direct_scores(dev, d):
+    """The precomputed int16 gather map gives the scores of the direct kernel
+    (same float16 features) and the oracle's gather geometry."""
+    import ctypes
+    from vesper_python_gb300 import _native
+    P = _prop()
+    from vesper_python_gb300 import vesper as vg
+    rng = np.random.default_rng(d)
+    angles = orc.calc_angle_comb(30.0)[::13]
+    mats_h = vg.rot_matrices(angles)
+    mats = dev.to_dev(mats_h)
+    sm = P.srcmap(dev, d, mats).cpu().numpy()
+    for r in range(len(angles)):
+        np.testing.assert_array_equal(sm[r].astype(np.int64), po.src_map(d, mats_h[r]))
+    K = 8
+    vm = dev.to_dev(rng.normal(size=(2, d ** 3, K)), torch.float16)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    a = torch.empty(len(angles), device=dev.device)
+    b = torch.empty(len(angles), device=dev.device)
+    _native.check(dev.lib.vesper_prop_score_f16(p(vm[0]), p(vm[1]), K, d, p(mats), len(angles), p(a), dev.stream))
+    smt = P.srcmap(dev, d, mats)
+    _native.check(dev.lib.vesper_prop_score_map(p(vm[0]), p(vm[1]), K, d, p(smt), len(angles), p(b), dev.stream))
+    np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())

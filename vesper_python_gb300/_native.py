@@ -104,6 +104,8 @@ SIGNATURES = {
     "vesper_fast_len_ok": [_i],
     "vesper_prepare_map": [_vp, _i, _i, _i, _d, _vp, _vp, _vp],
     "vesper_map_stats": [_vp, _i, _vp, _vp],
+    "vesper_map_stats_workspace_size": [_i, _psz],
+    "vesper_map_stats_ws": [_vp, _i, _vp, _vp, _sz, _vp],
     "vesper_fastvec_workspace_size": [_i, _i, _i, _i, _psz],
     "vesper_fastvec": [_vp, _i, _i, _i, _d, _vp, _i, _d, _vp, _d, _vp, _vp, _vp, _vp, _sz, _vp],
     "vesper_rot_gather": [_vp, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp],
@@ -127,6 +129,10 @@ SIGNATURES = {
     "vesper_prop_conv_fwd": [_vp, _i, _vp, _vp, _i, _i, _i, _i, _vp, _vp],
     "vesper_prop_vmajor": [_vp, _i, _i, _i, _vp, _vp],
     "vesper_prop_score_vm": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
+    "vesper_prop_vmajor_f16": [_vp, _i, _i, _i, _vp, _vp],
+    "vesper_prop_score_f16": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
+    "vesper_prop_srcmap": [_i, _vp, _i, _vp, _vp],
+    "vesper_prop_score_map": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
     "vesper_prop_conv_bwd": [_vp, _vp, _i, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp],
     "vesper_prop_score": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
     "vesper_prop_score_bwd_workspace": [_i, _i, _psz],

@@ -81,6 +81,20 @@ def _size_grid(dmax2_bits, count, cent, width, orig, s):
     return new_dim, new_orig, new_cent
 
 
+class _Pair:
+    """Per-pair state of align_many between its stages."""
+
+    def __init__(self, src1, src2, width1, width2, orig1, orig2):
+        self.src1, self.src2 = src1, src2
+        self.width1, self.width2 = width1, width2
+        self.orig1, self.orig2 = orig1, orig2
+        self.launches = 0
+        self.order = None
+        self.sub = None
+        self.z = None
+        self.fallback = False
+
+
 class Aligner:
     """Holds the device, cached angle-grid matrices and scratch buffers."""
 
@@ -92,8 +106,6 @@ class Aligner:
         self.profile = None      # set to a dict to collect per-pass search timings
         self.stages = None       # set to a dict to collect per-stage device milliseconds
         self._marks = []
-        self._prep = torch.empty(4, dtype=torch.int64, device=self.dev.device)
-        self._stats = torch.empty(5, dtype=torch.float64, device=self.dev.device)
 
     def _mark(self, name):
         """Event at a stage boundary (only while self.stages is a dict)."""
@@ -115,167 +127,229 @@ class Aligner:
         _native.check(self.lib.vesper_prepare_map(ctypes.c_void_p(src.data_ptr()), sx, sy, sz, float(th),
                                                   vg._host_d3(cent), ctypes.c_void_p(out.data_ptr()),
                                                   self.dev.stream))
-        self.launches += 2
 
     def align_device(self, src1, src2, width1, width2, orig1, orig2, p: AlignParams) -> AlignResult:
+        """One pair: ``align_many`` with a batch of one."""
+        return self.align_many([(src1, src2, width1, width2, orig1, orig2)], p)[0]
+
+    def align_many(self, items, p: AlignParams) -> list:
+        """Align a batch of pairs, items = [(src1, src2, width1, width2, orig1,
+        orig2)] with device maps of any (uneven) sizes.  Every stage is launched
+        for all pairs before the host waits, so the whole batch needs about five
+        host synchronisations instead of five per pair."""
         dev = self.dev
         mode = p.mode
         self.launches = 0
         self.d2h_bytes = 0
-        cent1 = np.array([s * 0.5 for s in src1.shape])
-        cent2 = np.array([s * 0.5 for s in src2.shape])
+        n = len(items)
+        if n == 0:
+            return []
+        P = [_Pair(*it) for it in items]
+        # ---- 1. threshold + radius (device), grid sizing (host) ----------------
         self._mark("prepare")
-        self._prepare(src1, p.t, cent1, self._prep[0:2])
-        self._prepare(src2, p.T, cent2, self._prep[2:4])
-        pr = self._prep.cpu().numpy().view(np.uint64)
-        self.d2h_bytes += self._prep.numel() * 8
-        o1 = np.array([np.float32(v) for v in orig1])
-        o2 = np.array([np.float32(v) for v in orig2])
-        d1, no1, c1 = _size_grid(pr[0], pr[1], cent1, width1, o1, p.s)
-        d2, no2, c2 = _size_grid(pr[2], pr[3], cent2, width2, o2, p.s)
-        if d1 > d2:
-            dim = d1
-            no2 = c2 - 0.5 * p.s * dim
-        else:
-            dim = d2
-            no1 = c1 - 0.5 * p.s * dim
+        prep = torch.empty((n, 4), dtype=torch.int64, device=dev.device)
+        for i, st in enumerate(P):
+            st.cent1 = np.array([x * 0.5 for x in st.src1.shape])
+            st.cent2 = np.array([x * 0.5 for x in st.src2.shape])
+            self._prepare(st.src1, p.t, st.cent1, prep[i, 0:2])
+            self._prepare(st.src2, p.T, st.cent2, prep[i, 2:4])
+            st.launches += 4
+        prh = prep.cpu().numpy().view(np.uint64)
+        self.d2h_bytes += prep.numel() * 8
+        # ---- 2. fastVEC, target statistics and spectra -------------------------
         self._mark("fastvec")
-        tdata, _, tvec = vg.fastvec_device(src1, np.float64(np.float32(width1)), o1.astype(np.float64), dim, p.s,
-                                           no1, p.g, dev=dev)
-        qdata, _, qvec = vg.fastvec_device(src2, np.float64(np.float32(width2)), o2.astype(np.float64), dim, p.s,
-                                           no2, p.g, dev=dev)
-        self.launches += 8
-        _native.check(self.lib.vesper_map_stats(ctypes.c_void_p(tdata.data_ptr()), dim,
-                                                ctypes.c_void_p(self._stats.data_ptr()), dev.stream))
-        self.launches += 1
-        stats = None
-        ave = 0.0
+        stats = torch.empty((n, 5), dtype=torch.float64, device=dev.device)
+        for i, st in enumerate(P):
+            o1 = np.array([np.float32(v) for v in st.orig1])
+            o2 = np.array([np.float32(v) for v in st.orig2])
+            d1, no1, st.c1 = _size_grid(prh[i, 0], prh[i, 1], st.cent1, st.width1, o1, p.s)
+            d2, no2, st.c2 = _size_grid(prh[i, 2], prh[i, 3], st.cent2, st.width2, o2, p.s)
+            if d1 > d2:
+                dim = d1
+                no2 = st.c2 - 0.5 * p.s * dim
+            else:
+                dim = d2
+                no1 = st.c1 - 0.5 * p.s * dim
+            st.dim = dim
+            st.tdata, _, st.tvec = vg.fastvec_device(st.src1, np.float64(np.float32(st.width1)),
+                                                     o1.astype(np.float64), dim, p.s, no1, p.g, dev=dev)
+            st.qdata, _, st.qvec = vg.fastvec_device(st.src2, np.float64(np.float32(st.width2)),
+                                                     o2.astype(np.float64), dim, p.s, no2, p.g, dev=dev)
+            ws = dev.workspace(("stats", dim), _native.size_query("vesper_map_stats_workspace_size", dim))
+            _native.check(self.lib.vesper_map_stats_ws(ctypes.c_void_p(st.tdata.data_ptr()), dim,
+                                                       ctypes.c_void_p(stats[i].data_ptr()),
+                                                       ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
+            st.launches += 12
+        sh = None
         if mode in ("PCC", "CC"):
-            stats = self._stats.cpu().numpy()
-            self.d2h_bytes += 40
-            ave = float(stats[2])
+            sh = stats.cpu().numpy()
+            self.d2h_bytes += sh.nbytes
         self._mark("spectra")
-        spec = vg.target_spectra_device(tdata, tvec, mode, ave, dev=dev)
-        self.launches += 2
+        for i, st in enumerate(P):
+            st.ave = float(sh[i, 2]) if sh is not None else 0.0
+            st.spec = vg.target_spectra_device(st.tdata, st.tvec, mode, st.ave, dev=dev)
+            st.launches += 2
+        # ---- 3. global pass: proposal subset or the whole grid -----------------
         angle_comb = vg.calc_angle_comb(p.A)
+        nang = len(angle_comb)
         mats = vg.rot_matrices_device(angle_comb, dev, key=("grid", float(p.A)))
-        grid_index = None
-        self.proposal_info = None
         if p.proposal is not None:
-            scores, lin, grid_index = self._proposal_pass(p, spec, tdata, tvec, qdata, qvec, mats, dim, ave)
-        if grid_index is None:
-            self._mark("search")
-            scores, lin = vg.search_device(spec, qdata, qvec, mode, ave, mats, batch=p.batch, dev=dev,
-                                           profile=self.profile, tuned=True)
-            self.launches += self._search_launches(dim, mode, len(angle_comb), p.batch)
-        top = vg.topn_device(scores, p.N, dev=dev)
-        self.launches += 1
-        raw = scores[:, 0].cpu().numpy()
-        lin_h = lin[:, 0].cpu().numpy()
-        top_h = [int(i) for i in top.cpu().numpy() if i >= 0]
-        self.d2h_bytes += raw.nbytes + lin_h.nbytes + top.numel() * 4
-        raw_grid, lin_grid = raw, lin_h
-        if grid_index is not None:
-            # subset positions -> grid indices (the subset is in ascending grid order)
-            gi = grid_index.cpu().numpy()
-            self.d2h_bytes += gi.nbytes
-            raw_grid = np.zeros(len(angle_comb), raw.dtype)
-            lin_grid = np.zeros(len(angle_comb), lin_h.dtype)
-            raw_grid[gi] = raw
-            lin_grid[gi] = lin_h
-            top_h = [int(gi[i]) for i in top_h]
-        if stats is None:
-            stats = self._stats.cpu().numpy()
-            self.d2h_bytes += 40
-        rd3 = 1.0 / dim ** 3
-        scale = 1.0
-        if mode == "CC":
-            scale = 1.0 / stats[3] ** 2
-        elif mode == "PCC":
-            scale = 1.0 / stats[4] ** 2
-        # statistics over the correlated rotations (the whole grid, or the subset)
-        score_arr = raw.astype(np.float64) * scale * rd3
-        ave_s, std_s = float(np.mean(score_arr)), float(np.std(score_arr))
-        score_grid = raw_grid.astype(np.float64) * scale * rd3
-        top_list = [(tuple(angle_comb[r]), float(score_grid[r]), vg.unravel(lin_grid[r], dim)) for r in top_h]
+            if mode != "VecProduct":
+                raise ValueError("the learned proposal ranks rotations for mode VecProduct only")
+            self._mark("proposal")
+            for st in P:
+                self._proposal_subset(p, st, mats)
+        self._mark("search")
+        for st in P:
+            self._global_search(p, st, mats if st.order is None else st.sub, nang)
+        zs = None
+        if p.proposal is not None:
+            zs = torch.stack([st.z for st in P]).cpu().numpy()
+            self.d2h_bytes += zs.nbytes
+            redo = [st for st, z in zip(P, zs) if p.proposal_fallback_z is not None and z < p.proposal_fallback_z]
+            for st in redo:       # the fallback: the whole grid
+                st.order = None
+                st.fallback = True
+                self._global_search(p, st, mats, nang)
+            self.proposal_info = {"subset": int(np.ceil(p.proposal_frac * nang)), "z": [float(z) for z in zs],
+                                  "fallback": [bool(st.fallback) for st in P]}
+        else:
+            self.proposal_info = None
+        if sh is None:
+            sh = stats.cpu().numpy()
+            self.d2h_bytes += sh.nbytes
+        # one wait for every pair's global results, then per pair: host
+        # bookkeeping and the refinement launch (the device works on pair i
+        # while the host prepares pair i+1)
+        glob = self._fetch([[st.scores[:, 0].contiguous(), st.lin[:, 0].contiguous(), st.top] +
+                            ([st.order] if st.order is not None else []) for st in P])
+        rd3s, scales = [], []
         if p.A > 5.0:
             self._mark("refine")
-            ref_angles = vg.refine_angle_list([angle_comb[r] for r in top_h])
-            rmats = dev.to_dev(vg.rot_matrices(ref_angles))
-            rs, rl = vg.search_device(spec, qdata, qvec, mode, ave, rmats, batch=p.batch, dev=dev, tuned=True)
-            self.launches += self._search_launches(dim, mode, len(ref_angles), p.batch)
-            rtop = vg.topn_device(rs, p.N, dev=dev)
-            self.launches += 1
-            rraw = rs[:, 0].cpu().numpy()
-            rlh = rl[:, 0].cpu().numpy()
-            self.d2h_bytes += rraw.nbytes + rlh.nbytes + rtop.numel() * 4
-            rtop = [int(i) for i in rtop.cpu().numpy() if i >= 0]
-            sel_angles = ref_angles[rtop]
-            entries = [(tuple(ref_angles[r]), float(np.float64(rraw[r]) * scale * rd3), vg.unravel(rlh[r], dim))
-                       for r in rtop]
-        else:
-            sel_angles = np.array([e[0] for e in top_list])
-            entries = top_list
-        models = []
+        for i, st in enumerate(P):
+            raw, lin_h, toph = glob[i][0], glob[i][1], glob[i][2]
+            top_h = [int(t) for t in toph if t >= 0]
+            raw_grid, lin_grid = raw, lin_h
+            if st.order is not None:
+                # subset positions -> grid indices (the subset is in ascending grid order)
+                gi = glob[i][3]
+                raw_grid = np.zeros(nang, raw.dtype)
+                lin_grid = np.zeros(nang, lin_h.dtype)
+                raw_grid[gi] = raw
+                lin_grid[gi] = lin_h
+                top_h = [int(gi[t]) for t in top_h]
+            rd3 = 1.0 / st.dim ** 3
+            scale = 1.0
+            if mode == "CC":
+                scale = 1.0 / sh[i, 3] ** 2
+            elif mode == "PCC":
+                scale = 1.0 / sh[i, 4] ** 2
+            rd3s.append(rd3)
+            scales.append(scale)
+            # statistics over the correlated rotations (the whole grid, or the subset)
+            score_arr = raw.astype(np.float64) * scale * rd3
+            st.ave_s, st.std_s = float(np.mean(score_arr)), float(np.std(score_arr))
+            score_grid = raw_grid.astype(np.float64) * scale * rd3
+            st.top_list = [(tuple(angle_comb[r]), float(score_grid[r]), vg.unravel(lin_grid[r], st.dim))
+                           for r in top_h]
+            st.top_h = top_h
+            # ---- 4. refinement around the pair's top-N ----------------------------
+            if p.A > 5.0:
+                st.ref_angles = vg.refine_angle_list([angle_comb[r] for r in st.top_h])
+                rmats = dev.to_dev_async(vg.rot_matrices(st.ref_angles))
+                st.rs, st.rl = vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats, batch=p.batch,
+                                                dev=dev, tuned=True)
+                st.launches += self._search_launches(st.dim, mode, len(st.ref_angles), p.batch)
+                st.rtop = vg.topn_device(st.rs, p.N, dev=dev)
+                st.launches += 1
+        # ---- 5. rotated top-N models and their float64 scores -------------------
+        if p.A > 5.0:
+            ref = self._fetch([[st.rs[:, 0].contiguous(), st.rl[:, 0].contiguous(), st.rtop] for st in P])
         self._mark("rescore")
-        if entries:
-            sel = dev.to_dev(vg.rot_matrices(sel_angles))
-            gd, gv, _ = vg.rot_gather_device(qdata, qvec, sel, dev=dev)
-            self.launches += 1
-            nm_ = len(entries)
-            res = torch.empty((nm_, 8), dtype=torch.float64, device=dev.device)
+        for i, st in enumerate(P):
+            if p.A > 5.0:
+                rraw, rlh, rtoph = ref[i]
+                rtop = [int(t) for t in rtoph if t >= 0]
+                st.sel_angles = st.ref_angles[rtop]
+                st.entries = [(tuple(st.ref_angles[r]), float(np.float64(rraw[r]) * scales[i] * rd3s[i]),
+                               vg.unravel(rlh[r], st.dim)) for r in rtop]
+            else:
+                st.sel_angles = np.array([e[0] for e in st.top_list])
+                st.entries = st.top_list
+            if not st.entries:
+                continue
+            dim = st.dim
+            sel = dev.to_dev_async(vg.rot_matrices(st.sel_angles))
+            gd, gv, _ = vg.rot_gather_device(st.qdata, st.qvec, sel, dev=dev)
+            nm_ = len(st.entries)
+            st.res = torch.empty((nm_, 8), dtype=torch.float64, device=dev.device)
             # translations wrapped to (-d/2, d/2] as get_score does (:1323-1329)
-            trw = np.array([[t - dim if t > 0.5 * dim else t for t in tr] for (_, _, tr) in entries], np.int32)
-            trd = dev.to_dev(trw)
-            ws = dev.workspace(("rescore", dim), _native.size_query("vesper_rescore_batch_workspace_size", dim, nm_))
+            trw = np.array([[t - dim if t > 0.5 * dim else t for t in tr] for (_, _, tr) in st.entries], np.int32)
+            trd = dev.to_dev_async(trw)
+            ws = torch.empty(_native.size_query("vesper_rescore_batch_workspace_size", dim, nm_), dtype=torch.uint8,
+                             device=dev.device)
             _native.check(self.lib.vesper_rescore_batch(
-                ctypes.c_void_p(tdata.data_ptr()), ctypes.c_void_p(tvec.data_ptr()), float(stats[2]),
-                float(stats[3]), float(stats[4]), ctypes.c_void_p(gd.data_ptr()), ctypes.c_void_p(gv.data_ptr()),
-                dim, ctypes.c_void_p(trd.data_ptr()), nm_, ctypes.c_void_p(res.data_ptr()),
+                ctypes.c_void_p(st.tdata.data_ptr()), ctypes.c_void_p(st.tvec.data_ptr()), float(sh[i, 2]),
+                float(sh[i, 3]), float(sh[i, 4]), ctypes.c_void_p(gd.data_ptr()), ctypes.c_void_p(gv.data_ptr()),
+                dim, ctypes.c_void_p(trd.data_ptr()), nm_, ctypes.c_void_p(st.res.data_ptr()),
                 ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
-            self.launches += 4
-            rh = res.cpu().numpy()
-            self.d2h_bytes += rh.nbytes
-            for k, (ang, sc, tr) in enumerate(entries):
-                r = vg.euler2rot(ang)
-                new_trans = vg.convert_trans(c1, c2, r, tr, p.s, dim)
-                nm, total = rh[k, 0], rh[k, 1]
-                models.append(Model(ang, sc, tr, new_trans, float(nm / total), float(rh[k, 2]), float(rh[k, 3]),
-                                    float(rh[k, 4])))
+            st.launches += 5
+        resh = self._fetch([[st.res] if st.entries else [] for st in P])
+        out = []
+        for i, st in enumerate(P):
+            models = []
+            if st.entries:
+                rh = resh[i][0]
+                for k, (ang, sc, tr) in enumerate(st.entries):
+                    r = vg.euler2rot(ang)
+                    new_trans = vg.convert_trans(st.c1, st.c2, r, tr, p.s, st.dim)
+                    nm, total = rh[k, 0], rh[k, 1]
+                    models.append(Model(ang, sc, tr, new_trans, float(nm / total), float(rh[k, 2]), float(rh[k, 3]),
+                                        float(rh[k, 4])))
+            self.launches += st.launches
+            out.append(AlignResult(st.dim, st.std_s, st.ave_s, st.top_list, models, st.launches))
         self._mark("end")
         self._close_marks()
-        return AlignResult(dim, std_s, ave_s, top_list, models, self.launches)
+        return out
 
-    def _proposal_pass(self, p, spec, tdata, tvec, qdata, qvec, mats, dim, ave):
-        """Global pass of the learned proposal: network scores of every
-        rotation, exact search of the best fraction.  Returns (scores, lin,
-        grid indices of the subset), or (None, None, None) when the fallback
-        rule sends the pair to the exhaustive search."""
+    def _fetch(self, groups):
+        """Device tensors (a list of lists) to numpy with one wait: the copies
+        are queued without blocking and the stream is synchronised once."""
+        outs = [[t.to("cpu", non_blocking=True) for t in g] for g in groups]
+        torch.cuda.current_stream(self.dev.device).synchronize()
+        res = [[o.numpy() for o in g] for g in outs]
+        self.d2h_bytes += sum(a.nbytes for g in res for a in g)
+        return res
+
+    def _proposal_subset(self, p, st, mats):
+        """Network scores of every rotation and the exact-search subset
+        (ascending grid indices) of one pair; all on the device."""
         from . import proposal as prop
-        if p.mode != "VecProduct":
-            raise ValueError("the learned proposal ranks rotations for mode VecProduct only")
         dev = self.dev
-        self._mark("proposal")
         pool = int(p.proposal_pool)
+        dim = st.dim
         dp = (dim + pool - 1) // pool
         fTQ = torch.empty((2, 4, dp, dp, dp), dtype=torch.float32, device=dev.device)
-        prop.map_field(tdata, tvec, pool, dev, out=fTQ[0])
-        prop.map_field(qdata, qvec, pool, dev, out=fTQ[1])
+        prop.map_field(st.tdata, st.tvec, pool, dev, out=fTQ[0])
+        prop.map_field(st.qdata, st.qvec, pool, dev, out=fTQ[1])
         s = p.proposal.rotation_scores(fTQ, mats)
-        order = prop.subset_from_scores(dev, s, p.proposal_frac).to(torch.int64)
-        sub = mats.index_select(0, order)
-        self._mark("search")
-        scores, lin = vg.search_device(spec, qdata, qvec, p.mode, ave, sub, batch=p.batch, dev=dev,
-                                       profile=self.profile, tuned=True)
-        self.launches += 2 + 4 + 1 + 1 + 1 + self._search_launches(dim, p.mode, int(order.numel()), p.batch)
-        sc0 = scores[:, 0]
-        z = float(((sc0.max() - sc0.mean()) / (sc0.std() + 1e-30)).item())
-        self.d2h_bytes += 4
-        self.proposal_info = {"subset": int(order.numel()), "z": z, "fallback": False}
-        if p.proposal_fallback_z is not None and z < p.proposal_fallback_z:
-            self.proposal_info["fallback"] = True
-            return None, None, None
-        return scores, lin, order
+        st.order = prop.subset_from_scores(dev, s, p.proposal_frac).to(torch.int64)
+        st.sub = mats.index_select(0, st.order)
+        st.launches += 9
+
+    def _global_search(self, p, st, mats, nang):
+        """Search of the given rotations, top-N and (subset searches) the
+        z-score of the best exact score over the subset; all on the device."""
+        st.scores, st.lin = vg.search_device(st.spec, st.qdata, st.qvec, p.mode, st.ave, mats, batch=p.batch,
+                                             dev=self.dev, profile=self.profile, tuned=True)
+        st.launches += self._search_launches(st.dim, p.mode, int(mats.shape[0]), p.batch)
+        st.top = vg.topn_device(st.scores, p.N, dev=self.dev)
+        st.launches += 1
+        if st.order is not None:
+            sc0 = st.scores[:, 0]
+            st.z = (sc0.max() - sc0.mean()) / (sc0.std() + 1e-30)
+        elif p.proposal is not None:
+            st.z = torch.zeros((), dtype=torch.float32, device=self.dev.device)
 
     def _search_launches(self, dim, mode, nrot, batch):
         if batch <= 0:
@@ -284,6 +358,15 @@ class Aligner:
             if t and t.get("batch"):
                 batch = int(t["batch"])
         return vg.search_plan(dim, mode, batch, nrot, None, self.dev)[1]
+
+    def align_host_many(self, items, p: AlignParams):
+        """End-to-end batch: items = [(host map1, host map2, width1, width2,
+        orig1, orig2)] with float32 [x][y][z] torch tensors (pinned for an
+        asynchronous copy) -> results."""
+        dev = self.dev
+        dev_items = [(h1.to(dev.device, non_blocking=True), h2.to(dev.device, non_blocking=True), w1, w2, o1, o2)
+                     for (h1, h2, w1, w2, o1, o2) in items]
+        return self.align_many(dev_items, p)
 
     def align_host(self, map1, map2, width1, width2, orig1, orig2, p: AlignParams, pinned=None):
         """End-to-end: host [x][y][z] float32 maps (pinned if given) -> results."""

@@ -82,9 +82,14 @@ __global__ void __launch_bounds__(256) k_fv_z(const float *src, const FvGeom g, 
     const size_t nrows = (size_t)g.S[0] * g.S[1];
     const size_t row0 = (size_t)blockIdx.x * kRB;
     float *rows = (float *)smem;
+    __shared__ int nz[kRB];   // row holds a non-zero value (thresholded maps are mostly empty rows)
+    if (threadIdx.x < kRB) nz[threadIdx.x] = 0;
+    __syncthreads();
     for (int e = threadIdx.x; e < kRB * S2; e += blockDim.x) {
         const size_t r = row0 + e / S2;
-        rows[e] = r < nrows ? src[r * S2 + (e % S2)] : 0.f;
+        const float v = r < nrows ? src[r * S2 + (e % S2)] : 0.f;
+        rows[e] = v;
+        if (v != 0.f) nz[e / S2] = 1;
     }
     __syncthreads();
     const int *stp = t.stp + 2 * d, *len = t.len + 2 * d;
@@ -93,6 +98,11 @@ __global__ void __launch_bounds__(256) k_fv_z(const float *src, const FvGeom g, 
         const int rr = o / d, z = o - rr * d;
         const size_t r = row0 + rr;
         if (r >= nrows) continue;
+        if (!nz[rr]) {   // an all-zero row: the sums are +0.0, as the loop would give
+            A0[r * d + z] = 0.0;
+            A1[r * d + z] = 0.0;
+            continue;
+        }
         const float *row = rows + rr * S2 + stp[z];
         const int n = len[z];
         double s0 = 0.0, s1 = 0.0;

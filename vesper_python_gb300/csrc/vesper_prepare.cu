@@ -95,6 +95,87 @@ __global__ void __launch_bounds__(kStThreads) k_stats(const double *data, size_t
     }
 }
 
+// The same statistics over many blocks: per-chunk partial sums in a
+// workspace, added in chunk order by one thread (deterministic), then the
+// centred norm the same way.  Float64 runs at a small fraction of the float32
+// rate on this part, so one block would leave the other SMs idle.
+constexpr int kSmThreads = 256;
+constexpr int kSmPerThread = 8;
+
+__device__ __forceinline__ void sm_chunk(size_t n, size_t &lo, size_t &hi) {
+    const size_t per = (size_t)kSmThreads * kSmPerThread;
+    lo = (size_t)blockIdx.x * per;
+    hi = lo + per < n ? lo + per : n;
+}
+
+__global__ void __launch_bounds__(kSmThreads) k_stats_p1(const double *data, size_t n, double *part) {
+    __shared__ double red[33];
+    size_t lo, hi;
+    sm_chunk(n, lo, hi);
+    double s = 0.0, cnt = 0.0, pos = 0.0, q = 0.0, np_ = 0.0;
+    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const double v = data[i];
+        s += v;
+        if (v != 0.0) cnt += 1.0;
+        if (v > 0.0) {
+            pos += v;
+            q += v * v;
+            np_ += 1.0;
+        }
+    }
+    s = st_block_sum(s, red);
+    cnt = st_block_sum(cnt, red);
+    pos = st_block_sum(pos, red);
+    q = st_block_sum(q, red);
+    np_ = st_block_sum(np_, red);
+    if (threadIdx.x == 0) {
+        double *p = part + (size_t)blockIdx.x * 6;
+        p[0] = s;
+        p[1] = cnt;
+        p[2] = pos;
+        p[3] = q;
+        p[4] = np_;
+    }
+}
+
+__global__ void k_stats_r1(const double *part, int nchunk, double *out) {
+    if (threadIdx.x != 0) return;
+    double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < nchunk; ++b)
+        for (int k = 0; k < 5; ++k) a[k] += part[(size_t)b * 6 + k];
+    out[0] = a[0];
+    out[1] = a[1];
+    out[2] = a[2] / a[4];
+    out[3] = sqrt(a[3]);
+}
+
+__global__ void __launch_bounds__(kSmThreads) k_stats_p2(const double *data, size_t n, const double *out,
+                                                         double *part) {
+    __shared__ double red[33];
+    size_t lo, hi;
+    sm_chunk(n, lo, hi);
+    const double ave = out[2];
+    double p2 = 0.0;
+    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const double v = data[i];
+        if (v > 0.0) p2 += (v - ave) * (v - ave);
+    }
+    p2 = st_block_sum(p2, red);
+    if (threadIdx.x == 0) part[(size_t)blockIdx.x * 6 + 5] = p2;
+}
+
+__global__ void k_stats_r2(const double *part, int nchunk, double *out) {
+    if (threadIdx.x != 0) return;
+    double p2 = 0.0;
+    for (int b = 0; b < nchunk; ++b) p2 += part[(size_t)b * 6 + 5];
+    out[4] = sqrt(p2);
+}
+
+static int stats_chunks(int dim) {
+    const size_t n = (size_t)dim * dim * dim, per = (size_t)kSmThreads * kSmPerThread;
+    return (int)((n + per - 1) / per);
+}
+
 }  // namespace vg
 
 using namespace vg;
@@ -114,9 +195,36 @@ extern "C" int vesper_prepare_map(float *data, int sx, int sy, int sz, double th
     return VESPER_OK;
 }
 
+extern "C" int vesper_map_stats_workspace_size(int dim, size_t *bytes) {
+    if (!bytes || dim < 1) return fail(VESPER_ERR_INVALID, "vesper_map_stats_workspace_size: bad arguments");
+    *bytes = (size_t)stats_chunks(dim) * 6 * sizeof(double);
+    return VESPER_OK;
+}
+
 extern "C" int vesper_map_stats(const double *data, int dim, double *stats_out, void *stream) {
     if (!data || !stats_out || dim < 1) return fail(VESPER_ERR_INVALID, "vesper_map_stats: bad arguments");
     k_stats<<<1, kStThreads, 0, (cudaStream_t)stream>>>(data, (size_t)dim * dim * dim, stats_out);
     VG_CHECK_LAUNCH("k_stats");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_map_stats_ws(const double *data, int dim, double *stats_out, void *workspace,
+                                   size_t workspace_bytes, void *stream) {
+    if (!data || !stats_out || dim < 1) return fail(VESPER_ERR_INVALID, "vesper_map_stats_ws: bad arguments");
+    size_t need = 0;
+    vesper_map_stats_workspace_size(dim, &need);
+    if (!workspace || workspace_bytes < need) return fail(VESPER_ERR_WORKSPACE, "vesper_map_stats_ws: workspace");
+    const size_t n = (size_t)dim * dim * dim;
+    const int nc = stats_chunks(dim);
+    double *part = (double *)workspace;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_stats_p1<<<nc, kSmThreads, 0, st>>>(data, n, part);
+    VG_CHECK_LAUNCH("k_stats_p1");
+    k_stats_r1<<<1, 32, 0, st>>>(part, nc, stats_out);
+    VG_CHECK_LAUNCH("k_stats_r1");
+    k_stats_p2<<<nc, kSmThreads, 0, st>>>(data, n, stats_out, part);
+    VG_CHECK_LAUNCH("k_stats_p2");
+    k_stats_r2<<<1, 32, 0, st>>>(part, nc, stats_out);
+    VG_CHECK_LAUNCH("k_stats_r2");
     return VESPER_OK;
 }

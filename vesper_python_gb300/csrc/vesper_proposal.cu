@@ -9,6 +9,7 @@
 // [Cout][Cin][27] stored as bfloat16 (3x3x3 taps, z fastest) with float32
 // accumulation; biases float32.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 
@@ -44,6 +45,50 @@ __global__ void k_conv_fwd(const float *in, int cin, const __nv_bfloat16 *W, con
         }
     }
     out[(size_t)co * n + v] = relu ? fmaxf(acc, 0.f) : acc;
+}
+
+// The same layer with COG output channels per thread: one input load feeds
+// COG products, the block's COG x cin x 27 weights sit in shared memory as
+// float32 (every thread reads the same weight at the same step: a broadcast),
+// and the 27 neighbour offsets and their in-grid mask are computed once per
+// voxel.  The summation order per output is that of k_conv_fwd (bias, then
+// ci, then tap), so the results are the same bits.
+template <int COG>
+__global__ void __launch_bounds__(128) k_conv_fwd_g(const float *in, int cin, const __nv_bfloat16 *W,
+                                                    const float *bias, int cout, int d, int relu, float *out) {
+    extern __shared__ float wsh[];   // [COG][cin][27]
+    const int n = d * d * d;
+    const int co0 = blockIdx.y * COG;
+    in += (size_t)blockIdx.z * cin * n;
+    out += (size_t)blockIdx.z * cout * n;
+    for (int i = threadIdx.x; i < COG * cin * 27; i += blockDim.x)
+        wsh[i] = __bfloat162float(W[(size_t)co0 * cin * 27 + i]);
+    __syncthreads();
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int x = v / (d * d), y = (v / d) % d, z = v % d;
+    uint32_t mask = 0u;
+#pragma unroll
+    for (int o = 0; o < 27; ++o) {
+        const int xx = x + o / 9 - 1, yy = y + (o / 3) % 3 - 1, zz = z + o % 3 - 1;
+        if (xx >= 0 && yy >= 0 && zz >= 0 && xx < d && yy < d && zz < d) mask |= 1u << o;
+    }
+    float acc[COG];
+#pragma unroll
+    for (int j = 0; j < COG; ++j) acc[j] = bias ? bias[co0 + j] : 0.f;
+    for (int ci = 0; ci < cin; ++ci) {
+        const float *src = in + (size_t)ci * n + v;
+        const float *w = wsh + ci * 27;
+#pragma unroll
+        for (int o = 0; o < 27; ++o) {
+            if (!(mask & (1u << o))) continue;
+            const float val = src[((o / 9 - 1) * d + ((o / 3) % 3 - 1)) * d + (o % 3 - 1)];
+#pragma unroll
+            for (int j = 0; j < COG; ++j) acc[j] = fmaf(w[j * cin * 27 + o], val, acc[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < COG; ++j) out[(size_t)(co0 + j) * n + v] = relu ? fmaxf(acc[j], 0.f) : acc[j];
 }
 
 // din[ci][v] = sum_co sum_o W[co][ci][o] * g[co][v - o],  g = dout (masked by
@@ -215,6 +260,159 @@ __global__ void k_prop_score_vm(const float4 *ET, const float4 *EQ, int d, const
         float t = 0.f;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
         scores[r] = t;
+    }
+}
+
+// [nmap][K][n] float32 -> [nmap][n][K] float16 (the inference features)
+__global__ void k_vmajor_f16(const float *in, int K, int n, __half *out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t per = (size_t)K * n;
+    if (i >= per) return;
+    const size_t m = blockIdx.y;
+    const int v = (int)(i / K), k = (int)(i % K);
+    out[m * per + i] = __float2half_rn(in[m * per + (size_t)k * n + (size_t)v]);
+}
+
+// Scores of RPB rotations per block from float16 voxel-major features, K8
+// groups of 8 channels (one 16-byte load per voxel and group): each target
+// voxel's features are loaded once for the block's RPB rotations, the
+// gathered query voxel once per rotation; products accumulate in float32.
+template <int K8, int RPB>
+__global__ void __launch_bounds__(256) k_prop_score_f16(const uint4 *ET, const uint4 *EQ, int d,
+                                                        const float *rotmats, int nrot, float *scores) {
+    __shared__ float F[RPB][9];
+    __shared__ float red[RPB][32];
+    const int r0 = blockIdx.x * RPB;
+    if (threadIdx.x < 9 * RPB) {
+        const int j = threadIdx.x / 9, e = threadIdx.x % 9;
+        F[j][e] = r0 + j < nrot ? rotmats[(size_t)(r0 + j) * 9 + e] : 0.f;
+    }
+    __syncthreads();
+    const int n = d * d * d;
+    float acc[RPB];
+#pragma unroll
+    for (int j = 0; j < RPB; ++j) acc[j] = 0.f;
+    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+        float2 t[K8][4];
+#pragma unroll
+        for (int g = 0; g < K8; ++g) {
+            const uint4 a = __ldg(ET + (size_t)v * K8 + g);
+            t[g][0] = __half22float2(*(const __half2 *)&a.x);
+            t[g][1] = __half22float2(*(const __half2 *)&a.y);
+            t[g][2] = __half22float2(*(const __half2 *)&a.z);
+            t[g][3] = __half22float2(*(const __half2 *)&a.w);
+        }
+#pragma unroll
+        for (int j = 0; j < RPB; ++j) {
+            if (r0 + j >= nrot) break;
+            const int s = prop_src(F[j], d, v);
+            if (s < 0) continue;
+#pragma unroll
+            for (int g = 0; g < K8; ++g) {
+                const uint4 b = __ldg(EQ + (size_t)s * K8 + g);
+                const float2 q0 = __half22float2(*(const __half2 *)&b.x), q1 = __half22float2(*(const __half2 *)&b.y);
+                const float2 q2 = __half22float2(*(const __half2 *)&b.z), q3 = __half22float2(*(const __half2 *)&b.w);
+                float a = acc[j];
+                a = fmaf(t[g][0].x, q0.x, a);
+                a = fmaf(t[g][0].y, q0.y, a);
+                a = fmaf(t[g][1].x, q1.x, a);
+                a = fmaf(t[g][1].y, q1.y, a);
+                a = fmaf(t[g][2].x, q2.x, a);
+                a = fmaf(t[g][2].y, q2.y, a);
+                a = fmaf(t[g][3].x, q3.x, a);
+                a = fmaf(t[g][3].y, q3.y, a);
+                acc[j] = a;
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < RPB; ++j) {
+        float a = acc[j];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) red[j][warp] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < RPB && r0 + (int)threadIdx.x < nrot) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+        scores[r0 + threadIdx.x] = t;
+    }
+}
+
+// Source voxel of every (rotation, destination voxel) of a small grid, as
+// int16 (-1: none): the rotation grid is fixed, so the gather geometry is
+// computed once and then streamed from HBM (nrot * d^3 * 2 bytes) instead of
+// being recomputed for every map pair.
+__global__ void k_prop_srcmap(int d, const float *rotmats, int nrot, int16_t *out) {
+    __shared__ float F[9];
+    const int r = blockIdx.y;
+    if (threadIdx.x < 9) F[threadIdx.x] = rotmats[(size_t)r * 9 + threadIdx.x];
+    __syncthreads();
+    const int n = d * d * d;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    out[(size_t)r * n + v] = (int16_t)prop_src(F, d, v);
+}
+
+// Scores from float16 voxel-major features and a precomputed source map:
+// RPB rotations per block, each target voxel's features loaded once for them.
+template <int K8, int RPB>
+__global__ void __launch_bounds__(256) k_prop_score_map(const uint4 *ET, const uint4 *EQ, int d,
+                                                        const int16_t *srcmap, int nrot, float *scores) {
+    __shared__ float red[RPB][32];
+    const int r0 = blockIdx.x * RPB;
+    const int n = d * d * d;
+    float acc[RPB];
+#pragma unroll
+    for (int j = 0; j < RPB; ++j) acc[j] = 0.f;
+    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+        int sj[RPB];
+#pragma unroll
+        for (int j = 0; j < RPB; ++j) sj[j] = r0 + j < nrot ? (int)__ldg(srcmap + (size_t)(r0 + j) * n + v) : -1;
+        float2 t[K8][4];
+#pragma unroll
+        for (int g = 0; g < K8; ++g) {
+            const uint4 a = __ldg(ET + (size_t)v * K8 + g);
+            t[g][0] = __half22float2(*(const __half2 *)&a.x);
+            t[g][1] = __half22float2(*(const __half2 *)&a.y);
+            t[g][2] = __half22float2(*(const __half2 *)&a.z);
+            t[g][3] = __half22float2(*(const __half2 *)&a.w);
+        }
+#pragma unroll
+        for (int j = 0; j < RPB; ++j) {
+            const int s = sj[j];
+            if (s < 0) continue;
+#pragma unroll
+            for (int g = 0; g < K8; ++g) {
+                const uint4 b = __ldg(EQ + (size_t)s * K8 + g);
+                const float2 q0 = __half22float2(*(const __half2 *)&b.x), q1 = __half22float2(*(const __half2 *)&b.y);
+                const float2 q2 = __half22float2(*(const __half2 *)&b.z), q3 = __half22float2(*(const __half2 *)&b.w);
+                float a = acc[j];
+                a = fmaf(t[g][0].x, q0.x, a);
+                a = fmaf(t[g][0].y, q0.y, a);
+                a = fmaf(t[g][1].x, q1.x, a);
+                a = fmaf(t[g][1].y, q1.y, a);
+                a = fmaf(t[g][2].x, q2.x, a);
+                a = fmaf(t[g][2].y, q2.y, a);
+                a = fmaf(t[g][3].x, q3.x, a);
+                a = fmaf(t[g][3].y, q3.y, a);
+                acc[j] = a;
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < RPB; ++j) {
+        float a = acc[j];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) red[j][warp] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < RPB && r0 + (int)threadIdx.x < nrot) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+        scores[r0 + threadIdx.x] = t;
     }
 }
 
@@ -438,6 +636,15 @@ extern "C" int vesper_prop_conv_fwd(const float *in, int cin, const void *W, con
     if (!in || !W || !out || cin < 1 || cout < 1 || d < 1 || nmap < 1 || nmap > 65535)
         return fail(VESPER_ERR_INVALID, "conv_fwd: bad args");
     const int n = d * d * d;
+    constexpr int COG = 4;
+    const size_t sm = (size_t)COG * cin * 27 * sizeof(float);
+    if (cout % COG == 0 && sm <= (size_t)smem_limit()) {
+        allow_smem(k_conv_fwd_g<COG>, sm);
+        k_conv_fwd_g<COG><<<dim3((n + 127) / 128, cout / COG, nmap), 128, sm, (cudaStream_t)stream>>>(
+            in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
+        VG_CHECK_LAUNCH("k_conv_fwd_g");
+        return VESPER_OK;
+    }
     k_conv_fwd<<<dim3((n + 127) / 128, cout, nmap), 128, 0, (cudaStream_t)stream>>>(
         in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
     VG_CHECK_LAUNCH("k_conv_fwd");
@@ -494,6 +701,69 @@ extern "C" int vesper_prop_score_vm(const float *ET, const float *EQ, int K, int
         default: return fail(VESPER_ERR_UNSUPPORTED, "prop_score_vm: K = %d", K);
     }
     VG_CHECK_LAUNCH("k_prop_score_vm");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_vmajor_f16(const float *in, int K, int d, int nmap, void *out, void *stream) {
+    if (!in || !out || K < 1 || d < 1 || nmap < 1 || nmap > 65535)
+        return fail(VESPER_ERR_INVALID, "vmajor_f16: bad args");
+    const size_t per = (size_t)K * d * d * d;
+    k_vmajor_f16<<<dim3((unsigned)((per + 255) / 256), nmap), 256, 0, (cudaStream_t)stream>>>(in, K, d * d * d,
+                                                                                              (__half *)out);
+    VG_CHECK_LAUNCH("k_vmajor_f16");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_score_f16(const void *ET, const void *EQ, int K, int d, const float *rotmats, int nrot,
+                                     float *scores, void *stream) {
+    if (!ET || !EQ || !rotmats || !scores || d < 1 || nrot < 0 || K < 8 || K % 8 || K > 32)
+        return fail(VESPER_ERR_INVALID, "prop_score_f16: bad args (K a multiple of 8, <= 32)");
+    if (((uintptr_t)ET | (uintptr_t)EQ) & 15) return fail(VESPER_ERR_INVALID, "prop_score_f16: 16-byte alignment");
+    if (nrot == 0) return VESPER_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    constexpr int RPB = 4;
+    const unsigned nb = (unsigned)((nrot + RPB - 1) / RPB);
+    const uint4 *a = (const uint4 *)ET, *b = (const uint4 *)EQ;
+    switch (K / 8) {
+        case 1: k_prop_score_f16<1, RPB><<<nb, 256, 0, st>>>(a, b, d, rotmats, nrot, scores); break;
+        case 2: k_prop_score_f16<2, RPB><<<nb, 256, 0, st>>>(a, b, d, rotmats, nrot, scores); break;
+        case 4: k_prop_score_f16<4, RPB><<<nb, 256, 0, st>>>(a, b, d, rotmats, nrot, scores); break;
+        default: return fail(VESPER_ERR_UNSUPPORTED, "prop_score_f16: K = %d", K);
+    }
+    VG_CHECK_LAUNCH("k_prop_score_f16");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_srcmap(int d, const float *rotmats, int nrot, void *srcmap_out, void *stream) {
+    if (!rotmats || !srcmap_out || d < 1 || nrot < 0 || nrot > 65535)
+        return fail(VESPER_ERR_INVALID, "prop_srcmap: bad args");
+    if ((long long)d * d * d > 32767) return fail(VESPER_ERR_UNSUPPORTED, "prop_srcmap: d^3 above int16");
+    if (nrot == 0) return VESPER_OK;
+    const int n = d * d * d;
+    k_prop_srcmap<<<dim3((n + 255) / 256, nrot), 256, 0, (cudaStream_t)stream>>>(d, rotmats, nrot,
+                                                                                (int16_t *)srcmap_out);
+    VG_CHECK_LAUNCH("k_prop_srcmap");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_score_map(const void *ET, const void *EQ, int K, int d, const void *srcmap, int nrot,
+                                     float *scores, void *stream) {
+    if (!ET || !EQ || !srcmap || !scores || d < 1 || nrot < 0 || K < 8 || K % 8 || K > 32)
+        return fail(VESPER_ERR_INVALID, "prop_score_map: bad args (K a multiple of 8, <= 32)");
+    if (((uintptr_t)ET | (uintptr_t)EQ) & 15) return fail(VESPER_ERR_INVALID, "prop_score_map: 16-byte alignment");
+    if (nrot == 0) return VESPER_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    constexpr int RPB = 4;
+    const unsigned nb = (unsigned)((nrot + RPB - 1) / RPB);
+    const uint4 *a = (const uint4 *)ET, *b = (const uint4 *)EQ;
+    const int16_t *m = (const int16_t *)srcmap;
+    switch (K / 8) {
+        case 1: k_prop_score_map<1, RPB><<<nb, 256, 0, st>>>(a, b, d, m, nrot, scores); break;
+        case 2: k_prop_score_map<2, RPB><<<nb, 256, 0, st>>>(a, b, d, m, nrot, scores); break;
+        case 4: k_prop_score_map<4, RPB><<<nb, 256, 0, st>>>(a, b, d, m, nrot, scores); break;
+        default: return fail(VESPER_ERR_UNSUPPORTED, "prop_score_map: K = %d", K);
+    }
+    VG_CHECK_LAUNCH("k_prop_score_map");
     return VESPER_OK;
 }
 

@@ -157,19 +157,31 @@ class ProposalNet:
                                                     self.b[i].numel(), lr, b1, b2, eps, self.step_count,
                                                     1.0 / batch, None, self.dev.stream))
 
-    def rotation_scores(self, fTQ, mats):
+    def rotation_scores(self, fTQ, mats, half=True):
         """Inference: both maps' fields stacked [2][4][d][d][d] -> score of
         every rotation (one encoder pass over the stack, voxel-major
-        features, vesper_prop_score_vm)."""
+        features: float16 with vesper_prop_score_f16, else float32 with
+        vesper_prop_score_vm)."""
         d = int(fTQ.shape[-1])
         K = CHANNELS[-1]
         feat = self.encode(fTQ, nmap=2)[-1]
-        vm = torch.empty((2, d * d * d, K), dtype=torch.float32, device=self.dev.device)
-        _native.check(self.lib.vesper_prop_vmajor(_p(feat), K, d, 2, _p(vm), self.dev.stream))
         n = int(mats.shape[0])
         s = torch.empty(n, dtype=torch.float32, device=self.dev.device)
-        _native.check(self.lib.vesper_prop_score_vm(_p(vm[0]), _p(vm[1]), K, d, _p(mats), n, _p(s),
-                                                    self.dev.stream))
+        if half:
+            vm = torch.empty((2, d * d * d, K), dtype=torch.float16, device=self.dev.device)
+            _native.check(self.lib.vesper_prop_vmajor_f16(_p(feat), K, d, 2, _p(vm), self.dev.stream))
+            sm = srcmap(self.dev, d, mats)
+            if sm is not None:
+                _native.check(self.lib.vesper_prop_score_map(_p(vm[0]), _p(vm[1]), K, d, _p(sm), n, _p(s),
+                                                             self.dev.stream))
+            else:
+                _native.check(self.lib.vesper_prop_score_f16(_p(vm[0]), _p(vm[1]), K, d, _p(mats), n, _p(s),
+                                                             self.dev.stream))
+        else:
+            vm = torch.empty((2, d * d * d, K), dtype=torch.float32, device=self.dev.device)
+            _native.check(self.lib.vesper_prop_vmajor(_p(feat), K, d, 2, _p(vm), self.dev.stream))
+            _native.check(self.lib.vesper_prop_score_vm(_p(vm[0]), _p(vm[1]), K, d, _p(mats), n, _p(s),
+                                                        self.dev.stream))
         return s
 
     def propose(self, fTQ, mats, frac):
@@ -177,6 +189,29 @@ class ProposalNet:
         rotations, and the scores of all of them."""
         s = self.rotation_scores(fTQ, mats)
         return subset_from_scores(self.dev, s, frac), s
+
+
+_SRCMAPS = {}
+SRCMAP_BUDGET = 2 << 30      # bytes of cached gather maps (HBM is plentiful; each is nrot * d^3 * 2)
+
+
+def srcmap(dev, d, mats):
+    """Cached int16 gather map [nrot][d^3] of this rotation set on a d^3 grid
+    (vesper_prop_srcmap), or None when d^3 exceeds int16 or the cache budget."""
+    n = int(mats.shape[0])
+    if d ** 3 > 32767:
+        return None
+    # the entry keeps the rotation tensor alive, so its address names it
+    key = (dev.device, d, mats.data_ptr(), n)
+    ent = _SRCMAPS.get(key)
+    if ent is None:
+        need = n * d ** 3 * 2
+        if sum(m.numel() * 2 for _, m in _SRCMAPS.values()) + need > SRCMAP_BUDGET:
+            return None
+        m = torch.empty((n, d ** 3), dtype=torch.int16, device=dev.device)
+        _native.check(dev.lib.vesper_prop_srcmap(d, _p(mats), n, _p(m), dev.stream))
+        ent = _SRCMAPS[key] = (mats, m)
+    return ent[1]
 
 
 def target_distribution(scores, beta):
@@ -268,9 +303,10 @@ class PairMaker:
         al = self.al
         cent1 = np.array([x * 0.5 for x in m1.shape])
         cent2 = np.array([x * 0.5 for x in m2.shape])
-        al._prepare(m1, self.t, cent1, al._prep[0:2])
-        al._prepare(m2, self.t, cent2, al._prep[2:4])
-        pr = al._prep.cpu().numpy().view(np.uint64)
+        prep = torch.empty(4, dtype=torch.int64, device=self.dev.device)
+        al._prepare(m1, self.t, cent1, prep[0:2])
+        al._prepare(m2, self.t, cent2, prep[2:4])
+        pr = prep.cpu().numpy().view(np.uint64)
         oo1 = np.array([np.float32(v) for v in o1])
         oo2 = np.array([np.float32(v) for v in o2])
         d1, no1, c1 = align._size_grid(pr[0], pr[1], cent1, 1.0, oo1, self.s)

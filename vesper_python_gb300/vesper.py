@@ -67,6 +67,13 @@ class Device:
             self._ws[key] = buf
         return buf
 
+    def to_dev_async(self, a):
+        """Small host array -> device without waiting on the stream: staged in
+        pinned memory (torch's caching host allocator keeps the staging block
+        until the copy has run)."""
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t.to(self.device, non_blocking=True)
+
     def to_dev(self, a, dtype=None):
         t = torch.as_tensor(np.ascontiguousarray(a))
         if dtype is not None:
