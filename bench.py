@@ -303,13 +303,15 @@ def run_gb300(args):
     ach_flop = pm[names[top]]["flop"] * per_launch_rot / avg_s / 1e12
     sm_mhz = clocks.get("sm_mhz") or 1900.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    # DRAM bytes of the kernel per launch: the ncu capture's bytes per rotation
+    # (profiles/traffic_<workload>.txt) times the rotations of an average launch
     traffic = None
     tr_path = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.txt")
     if os.path.exists(tr_path) and args.mode == "V":
         for ln in open(tr_path):
             f = ln.split()
             if len(f) == 2 and not ln.startswith("#") and f[0] == names[top]:
-                traffic = int(f[1])
+                traffic = int(round(float(f[1]) * per_launch_rot))
     kname = {0: "k_pass_", 1: "k_rpass_", 2: "k_fused"}[plan_path]
     kname = kname + names[top][-1] if plan_path != 2 else kname
     if use_prop:

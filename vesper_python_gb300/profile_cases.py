@@ -1,0 +1,56 @@
+"""Small, self-contained cases for profiler captures of single kernels.
+
+  python -m vesper_python_gb300.profile_cases search<d> [nrot]
+      three register/fused-path searches of seeded random side-d fields over
+      the first nrot (default 1008) rotations of the 30-degree grid
+  python -m vesper_python_gb300.profile_cases prop
+      three learned-proposal scorings (committed weights) of one held-out
+      128^3 / 64^3 pair at s = 3 over the 10-degree grid
+
+Each run is a few GPU milliseconds, so a capture of one of its launches ends
+in seconds.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+import torch
+
+from . import proposal as P
+from . import vesper as vg
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    dev = vg.default_device()
+    what = argv[0]
+    if what.startswith("search"):
+        d = int(what[6:])
+        nrot = int(argv[1]) if len(argv) > 1 else 1008
+        rng = np.random.default_rng(d)
+        data = rng.uniform(0.1, 2, size=(d, d, d))
+        data[rng.random((d, d, d)) < 0.5] = 0
+        vec = rng.normal(size=(d, d, d, 3))
+        vec /= np.linalg.norm(vec, axis=-1, keepdims=True)
+        vec[data == 0] = 0
+        td, tv = dev.to_dev(data), dev.to_dev(vec.astype(np.float32))
+        spec = vg.target_spectra_device(td, tv, "VecProduct", 0.0, dev=dev)
+        mats = dev.to_dev(vg.rot_matrices(vg.calc_angle_comb(30.0)[:nrot]))
+        for _ in range(3):
+            vg.search_device(spec, td, tv, "VecProduct", 0.0, mats, dev=dev, tuned=True)
+    elif what == "prop":
+        net = P.load_weights(dev)[0]
+        maker = P.PairMaker(dev)
+        mats = vg.rot_matrices_device(vg.calc_angle_comb(10.0), dev, key=("grid", 10.0))
+        pf = maker.fields(30_000_000)
+        for _ in range(3):
+            net.rotation_scores(pf.fTQ, mats)
+    else:
+        raise SystemExit(f"unknown case {what!r}")
+    torch.cuda.synchronize()
+    print("ok", what)
+
+
+if __name__ == "__main__":
+    main()
