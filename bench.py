@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=WORKLOAD, choices=["prop128_s3_a10", "pair200_s2_a10"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=["prop128_s3_a10", "pair200_s2_a10", "uneven64_s4_a15"])
     ap.add_argument("--pairs", type=int, default=16, help="pairs per step (prop128_s3_a10)")
     ap.add_argument("--mode", default="V", choices=list("VOCPL"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -352,6 +352,114 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def run_uneven(args):
+    """64 pairs of uneven sizes (map1 side in {64..256}, map2 = map1 / 2, blob
+    count proportional to volume) at s = 4, A = 15, exhaustive search: one
+    align_many call per step with the global stage replayed as one CUDA graph.
+    Reports alignments/s and the per-pair latency (batch start to the pair's
+    last kernel, device events) p50/p99; also the same batch without the
+    graph and each pair aligned alone."""
+    import torch
+    from vesper_python_gb300 import align, proposal, synth
+    from vesper_python_gb300 import vesper as vg
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = vg.Device(f"cuda:{local}")
+    w = synth.UNEVEN_WORKLOAD
+    p = align.AlignParams(t=w["t"], T=w["T"], g=w["g"], s=w["s"], A=w["A"], N=w["N"])
+    items, host_items, sides = [], [], []
+    for i in range(w["pairs"]):
+        seed, side, nblob, radius = synth.uneven_spec(i + rank * w["pairs"])
+        m1, m2, o1, o2 = proposal.blob_pair_torch(seed, side=side, nblob=nblob, radius=radius, device=dev.device)
+        items.append((m1, m2, 1.0, 1.0, o1, o2))
+        host_items.append((m1.cpu().pin_memory(), m2.cpu().pin_memory(), 1.0, 1.0, o1, o2))
+        sides.append(side)
+    al = align.Aligner(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev.device)
+
+    def timed(graph, steps, warmup):
+        for _ in range(warmup):
+            al.align_many(items, p, graph)
+        torch.cuda.synchronize()
+        lat = []
+        launches = 0
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        total = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            al.pair_events = []
+            e0.record()
+            res = al.align_many(items, p, graph)
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+            lat += [e0.elapsed_time(e) for e in al.pair_events]
+            launches += al.launches
+            al.pair_events = None
+        return total / steps, np.array(lat), launches, res
+
+    clk = ClockSampler(local)
+    clk.start()
+    ms, lat, launches, res = timed(True, args.steps, args.warmup)
+    clocks = clk.stop()
+    ms_ng, lat_ng, _, res_ng = timed(False, max(1, args.steps), 1)
+    same = all(a.top == b.top and [m.dot_score for m in a.models] == [m.dot_score for m in b.models]
+               for a, b in zip(res, res_ng))
+    # e2e: maps copied from pinned host memory every step
+    al.align_host_many(host_items, p, True)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    d2h = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        al.align_host_many(host_items, p, True)
+        d2h += al.d2h_bytes
+    t1.record()
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1) / args.steps
+    # each pair alone (one align_device per pair)
+    solo = []
+    for it in items:
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record()
+        al.align_device(*it, p)
+        a1.record()
+        torch.cuda.synchronize()
+        solo.append(a0.elapsed_time(a1))
+    solo = np.array(solo)
+    n = len(items)
+    dims = sorted({r.dim for r in res})
+    pct = lambda a, q: round(float(np.percentile(a, q)), 3)
+    line = {
+        "metric": METRIC, "value": round(n / (ms / 1e3), 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 fastVEC, target spectra, rescoring)",
+        "data": "synthetic (seeded blob-map pairs of uneven sizes at 1 A, generated on the GPU)",
+        "config": {"workload": f"uneven64_s4_a15: {n} pairs per step, map1 side in {sorted(set(sides))} "
+                               f"(map2 = side/2, blobs proportional to volume), s=4, A=15 "
+                               f"({len(vg.calc_angle_comb(p.A))} rotations + refinement), g=16, N=10, mode V, "
+                               f"exhaustive search, global stage as one CUDA graph",
+                   "grid_sides": dims, "pairs_per_step": n,
+                   "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{world}"},
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "note": "batch start to the pair's last kernel"},
+        "without_graph": {"value": round(n / (ms_ng / 1e3), 4), "latency_p50_ms": pct(lat_ng, 50),
+                          "latency_p99_ms": pct(lat_ng, 99), "same_results": bool(same)},
+        "one_pair_at_a_time": {"value": round(n / (solo.sum() / 1e3), 4), "latency_p50_ms": pct(solo, 50),
+                               "latency_p99_ms": pct(solo, 99)},
+        "graph": {"captures": al.graph_captures, "replays": al.graph_replays},
+        "e2e": {"value": round(n / (e2e_ms / 1e3), 4), "unit": UNIT,
+                "h2d_bytes_per_step": int(sum(h1.numel() * 4 + h2.numel() * 4 for (h1, h2, *_r) in host_items)),
+                "d2h_bytes_per_step": int(d2h / args.steps)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def cpu_baseline(args, threads, budget_s):
     """The reference algorithm on this host's CPU (the oracle restatement,
     exhaustive search like the reference), timed on a bounded sample and
@@ -432,5 +540,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "uneven64_s4_a15":
+        run_uneven(a)
     else:
         run_gb300(a)

@@ -106,6 +106,10 @@ class Aligner:
         self.profile = None      # set to a dict to collect per-pass search timings
         self.stages = None       # set to a dict to collect per-stage device milliseconds
         self._marks = []
+        self._graphs = {}        # batch signature -> (CUDA graph, its statistics, per-pair outputs)
+        self.graph_captures = 0
+        self.graph_replays = 0
+        self.pair_events = None  # set to a list to get one event per pair after its last kernel
 
     def _mark(self, name):
         """Event at a stage boundary (only while self.stages is a dict)."""
@@ -132,7 +136,7 @@ class Aligner:
         """One pair: ``align_many`` with a batch of one."""
         return self.align_many([(src1, src2, width1, width2, orig1, orig2)], p)[0]
 
-    def align_many(self, items, p: AlignParams) -> list:
+    def align_many(self, items, p: AlignParams, graph: bool = False) -> list:
         """Align a batch of pairs, items = [(src1, src2, width1, width2, orig1,
         orig2)] with device maps of any (uneven) sizes.  Every stage is launched
         for all pairs before the host waits, so the whole batch needs about five
@@ -157,51 +161,29 @@ class Aligner:
         prh = prep.cpu().numpy().view(np.uint64)
         self.d2h_bytes += prep.numel() * 8
         # ---- 2. fastVEC, target statistics and spectra -------------------------
-        self._mark("fastvec")
-        stats = torch.empty((n, 5), dtype=torch.float64, device=dev.device)
         for i, st in enumerate(P):
-            o1 = np.array([np.float32(v) for v in st.orig1])
-            o2 = np.array([np.float32(v) for v in st.orig2])
-            d1, no1, st.c1 = _size_grid(prh[i, 0], prh[i, 1], st.cent1, st.width1, o1, p.s)
-            d2, no2, st.c2 = _size_grid(prh[i, 2], prh[i, 3], st.cent2, st.width2, o2, p.s)
+            st.o1 = np.array([np.float32(v) for v in st.orig1])
+            st.o2 = np.array([np.float32(v) for v in st.orig2])
+            d1, st.no1, st.c1 = _size_grid(prh[i, 0], prh[i, 1], st.cent1, st.width1, st.o1, p.s)
+            d2, st.no2, st.c2 = _size_grid(prh[i, 2], prh[i, 3], st.cent2, st.width2, st.o2, p.s)
             if d1 > d2:
-                dim = d1
-                no2 = st.c2 - 0.5 * p.s * dim
+                st.dim = d1
+                st.no2 = st.c2 - 0.5 * p.s * st.dim
             else:
-                dim = d2
-                no1 = st.c1 - 0.5 * p.s * dim
-            st.dim = dim
-            st.tdata, _, st.tvec = vg.fastvec_device(st.src1, np.float64(np.float32(st.width1)),
-                                                     o1.astype(np.float64), dim, p.s, no1, p.g, dev=dev)
-            st.qdata, _, st.qvec = vg.fastvec_device(st.src2, np.float64(np.float32(st.width2)),
-                                                     o2.astype(np.float64), dim, p.s, no2, p.g, dev=dev)
-            ws = dev.workspace(("stats", dim), _native.size_query("vesper_map_stats_workspace_size", dim))
-            _native.check(self.lib.vesper_map_stats_ws(ctypes.c_void_p(st.tdata.data_ptr()), dim,
-                                                       ctypes.c_void_p(stats[i].data_ptr()),
-                                                       ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
-            st.launches += 12
-        sh = None
-        if mode in ("PCC", "CC"):
-            sh = stats.cpu().numpy()
-            self.d2h_bytes += sh.nbytes
-        self._mark("spectra")
-        for i, st in enumerate(P):
-            st.ave = float(sh[i, 2]) if sh is not None else 0.0
-            st.spec = vg.target_spectra_device(st.tdata, st.tvec, mode, st.ave, dev=dev)
-            st.launches += 2
-        # ---- 3. global pass: proposal subset or the whole grid -----------------
+                st.dim = d2
+                st.no1 = st.c1 - 0.5 * p.s * st.dim
         angle_comb = vg.calc_angle_comb(p.A)
         nang = len(angle_comb)
         mats = vg.rot_matrices_device(angle_comb, dev, key=("grid", float(p.A)))
-        if p.proposal is not None:
-            if mode != "VecProduct":
-                raise ValueError("the learned proposal ranks rotations for mode VecProduct only")
-            self._mark("proposal")
-            for st in P:
-                self._proposal_subset(p, st, mats)
-        self._mark("search")
-        for st in P:
-            self._global_search(p, st, mats if st.order is None else st.sub, nang)
+        if p.proposal is not None and mode != "VecProduct":
+            raise ValueError("the learned proposal ranks rotations for mode VecProduct only")
+        # ---- 2-3. fastVEC, statistics, spectra, global pass (one CUDA graph per
+        # batch signature when graph=True: the stage needs no host value
+        # between its launches except in modes CC/PCC) --------------------------
+        if graph and mode not in ("PCC", "CC"):
+            stats, sh = self._global_stage_graph(P, p, mats, nang), None
+        else:
+            stats, sh = self._global_stage(P, p, mats, nang)
         zs = None
         if p.proposal is not None:
             zs = torch.stack([st.z for st in P]).cpu().numpy()
@@ -294,6 +276,10 @@ class Aligner:
                 dim, ctypes.c_void_p(trd.data_ptr()), nm_, ctypes.c_void_p(st.res.data_ptr()),
                 ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
             st.launches += 5
+            if self.pair_events is not None:
+                e = torch.cuda.Event(enable_timing=True)
+                e.record()
+                self.pair_events.append(e)
         resh = self._fetch([[st.res] if st.entries else [] for st in P])
         out = []
         for i, st in enumerate(P):
@@ -311,6 +297,89 @@ class Aligner:
         self._mark("end")
         self._close_marks()
         return out
+
+    def _global_stage(self, P, p, mats, nang):
+        """fastVEC of both maps, target statistics and spectra, proposal subset
+        and global search of every pair (device work only, except the
+        statistics read that modes CC/PCC need before their spectra)."""
+        dev = self.dev
+        mode = p.mode
+        n = len(P)
+        self._mark("fastvec")
+        stats = torch.empty((n, 5), dtype=torch.float64, device=dev.device)
+        for i, st in enumerate(P):
+            dim = st.dim
+            st.tdata, _, st.tvec = vg.fastvec_device(st.src1, np.float64(np.float32(st.width1)),
+                                                     st.o1.astype(np.float64), dim, p.s, st.no1, p.g, dev=dev)
+            st.qdata, _, st.qvec = vg.fastvec_device(st.src2, np.float64(np.float32(st.width2)),
+                                                     st.o2.astype(np.float64), dim, p.s, st.no2, p.g, dev=dev)
+            ws = dev.workspace(("stats", dim), _native.size_query("vesper_map_stats_workspace_size", dim))
+            _native.check(self.lib.vesper_map_stats_ws(ctypes.c_void_p(st.tdata.data_ptr()), dim,
+                                                       ctypes.c_void_p(stats[i].data_ptr()),
+                                                       ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
+            st.launches += 12
+        sh = None
+        if mode in ("PCC", "CC"):
+            sh = stats.cpu().numpy()
+            self.d2h_bytes += sh.nbytes
+        self._mark("spectra")
+        for i, st in enumerate(P):
+            st.ave = float(sh[i, 2]) if sh is not None else 0.0
+            st.spec = vg.target_spectra_device(st.tdata, st.tvec, mode, st.ave, dev=dev)
+            st.launches += 2
+        if p.proposal is not None:
+            self._mark("proposal")
+            for st in P:
+                self._proposal_subset(p, st, mats)
+        self._mark("search")
+        for st in P:
+            self._global_search(p, st, mats if st.order is None else st.sub, nang)
+        return stats, sh
+
+    _STAGE_FIELDS = ("tdata", "tvec", "qdata", "qvec", "ave", "spec", "order", "sub", "scores", "lin", "top", "z",
+                     "launches")
+
+    def _global_stage_graph(self, P, p, mats, nang):
+        """_global_stage through a CUDA graph cached by the batch's signature
+        (input addresses and shapes, grid geometry, parameters): a repeated
+        batch replays one graph instead of its hundreds of launches.  A new
+        signature runs the stage once eagerly (autotuning, first launches),
+        then captures it."""
+        sig = (tuple((st.src1.data_ptr(), st.src2.data_ptr(), tuple(st.src1.shape), tuple(st.src2.shape), st.dim,
+                      tuple(np.asarray(st.no1, np.float64)), tuple(np.asarray(st.no2, np.float64)),
+                      float(st.width1), float(st.width2), tuple(st.o1), tuple(st.o2)) for st in P),
+               (p.t, p.T, p.g, p.s, p.A, p.N, p.mode, p.batch, id(p.proposal), p.proposal_frac, p.proposal_pool),
+               mats.data_ptr())
+        ent = self._graphs.get(sig)
+        if ent is None:
+            base = [st.launches for st in P]
+            self._global_stage(P, p, mats, nang)           # warm-up: tunes, loads kernels, fills caches
+            marks, self.stages = self.stages, None
+            for st, b0 in zip(P, base):
+                st.launches = b0
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                stats, _ = self._global_stage(P, p, mats, nang)
+            self.stages = marks
+            saved = []
+            for st, b0 in zip(P, base):
+                sv = {k: getattr(st, k) for k in self._STAGE_FIELDS}
+                sv["launches"] = st.launches - b0          # launches inside the graph
+                st.launches = b0
+                saved.append(sv)
+            ent = self._graphs[sig] = (g, stats, saved)
+            self.graph_captures += 1
+        g, stats, saved = ent
+        self._mark("global")
+        g.replay()
+        for st, sv in zip(P, saved):
+            for k in self._STAGE_FIELDS:
+                if k == "launches":
+                    st.launches += sv[k]
+                else:
+                    setattr(st, k, sv[k])
+        self.graph_replays += 1
+        return stats
 
     def _fetch(self, groups):
         """Device tensors (a list of lists) to numpy with one wait: the copies
@@ -359,14 +428,14 @@ class Aligner:
                 batch = int(t["batch"])
         return vg.search_plan(dim, mode, batch, nrot, None, self.dev)[1]
 
-    def align_host_many(self, items, p: AlignParams):
+    def align_host_many(self, items, p: AlignParams, graph: bool = False):
         """End-to-end batch: items = [(host map1, host map2, width1, width2,
         orig1, orig2)] with float32 [x][y][z] torch tensors (pinned for an
         asynchronous copy) -> results."""
         dev = self.dev
         dev_items = [(h1.to(dev.device, non_blocking=True), h2.to(dev.device, non_blocking=True), w1, w2, o1, o2)
                      for (h1, h2, w1, w2, o1, o2) in items]
-        return self.align_many(dev_items, p)
+        return self.align_many(dev_items, p, graph)
 
     def align_host(self, map1, map2, width1, width2, orig1, orig2, p: AlignParams, pinned=None):
         """End-to-end: host [x][y][z] float32 maps (pinned if given) -> results."""

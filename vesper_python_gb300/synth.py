@@ -149,6 +149,17 @@ WORKLOADS = {
 }
 
 UNEVEN_SIDES = (64, 96, 128, 160, 192, 256)
+UNEVEN_WORKLOAD = dict(pairs=64, t=0.1, T=0.1, g=16.0, s=4.0, A=15.0, N=10)
+
+
+def uneven_spec(index, seed_base=1000):
+    """(generator seed, map1 side, blob count, sphere radius) of pair ``index``
+    of the uneven batch: side drawn from UNEVEN_SIDES, blob count
+    proportional to volume, radius proportional to side."""
+    rng = np.random.default_rng(seed_base + index)
+    side = int(rng.choice(UNEVEN_SIDES))
+    scale = side / 128.0
+    return seed_base * 7 + index, side, max(8, int(round(400 * scale ** 3))), 40.0 * scale
 
 
 def workload_pair(name, seed=0):
@@ -158,10 +169,6 @@ def workload_pair(name, seed=0):
 
 
 def uneven_pair(index, seed_base=1000):
-    """One pair of the uneven batch: side drawn from UNEVEN_SIDES, blob count
-    proportional to volume, sphere radius proportional to side."""
-    rng = np.random.default_rng(seed_base + index)
-    side = int(rng.choice(UNEVEN_SIDES))
-    scale = side / 128.0
-    nblob = max(8, int(round(400 * scale ** 3)))
-    return make_pair(seed_base * 7 + index, side, nblob, 40.0 * scale)
+    """One pair of the uneven batch (uneven_spec), generated with numpy."""
+    seed, side, nblob, radius = uneven_spec(index, seed_base)
+    return make_pair(seed, side, nblob, radius)
