@@ -290,7 +290,8 @@ def test_topn_stable_ties(dev):
     assert list(out) == [1, 2, 4, 3, 6, 0, 5, -1, -1]
 
 
-@pytest.mark.parametrize("d,stride", [(13, 1), (28, 101), (30, 101), (32, 101), (75, 97)])
+@pytest.mark.parametrize("d,stride", [(13, 1), (27, 101), (28, 101), (30, 101), (32, 101), (33, 101), (35, 101),
+                                      (42, 211), (44, 211), (75, 97)])
 def test_register_fft_path_vs_oracle_and_radix_path(dev, d, stride):
     """The register two-step passes (compiled for these sides in mode V)
     against the oracle and against the radix-stage passes."""
@@ -314,7 +315,7 @@ def test_register_fft_path_vs_oracle_and_radix_path(dev, d, stride):
     assert np.max(np.abs(out[0][0] - out[1][0])) <= SCORE_RTOL * np.max(np.abs(osc))
 
 
-@pytest.mark.parametrize("d,stride", [(8, 7), (9, 7), (12, 3), (13, 1), (16, 5), (21, 11), (24, 13)])
+@pytest.mark.parametrize("d,stride", [(8, 7), (9, 7), (11, 7), (12, 3), (13, 1), (16, 5), (21, 11), (24, 13)])
 def test_fused_search_vs_oracle_and_pass_path(dev, d, stride):
     """The fused single-kernel search (compiled sides, mode V) against the
     oracle and against the radix-stage passes on the same rotations."""

@@ -5,7 +5,7 @@
 // and one launch for every rotation of the grid (a persistent grid-stride
 // loop over rotations).  Each line FFT runs whole in one thread's registers
 // (rdft<D>, D <= 32), so D is a compile-time side; the sides and modes
-// compiled are in the table at the end (mode V for 8 <= D <= 24, the scalar
+// compiled are in the table at the end (mode V for the sides 8 to 24, the scalar
 // modes O/C/P/L for 12 <= D <= 16, the grids of 128^3/64^3 pairs at s = 7).  It computes the same quantities as the three-pass
 // search (vesper_search.cu) in a different FFT order, so scores agree to
 // float32 rounding, not bit for bit.
@@ -220,6 +220,7 @@ constexpr FusedEntry fused_entry() {
 
 static const FusedEntry kFused[] = {
     fused_entry<VESPER_MODE_VEC, 3, 8>(),  fused_entry<VESPER_MODE_VEC, 3, 9>(),
+    fused_entry<VESPER_MODE_VEC, 3, 11>(),
     fused_entry<VESPER_MODE_VEC, 3, 10>(), fused_entry<VESPER_MODE_VEC, 3, 12>(),
     fused_entry<VESPER_MODE_VEC, 3, 13>(), fused_entry<VESPER_MODE_VEC, 3, 14>(),
     fused_entry<VESPER_MODE_VEC, 3, 15>(), fused_entry<VESPER_MODE_VEC, 3, 16>(),

@@ -411,8 +411,9 @@ struct RegPath {
     }
 };
 
-// Lookups of the tables in vesper_regsearch_a.cu / vesper_regsearch_b.cu.
+// Lookups of the tables in vesper_regsearch_{a,b,c}.cu.
 const RegEntry *find_reg_a(int mode, int d);
 const RegEntry *find_reg_b(int mode, int d);
+const RegEntry *find_reg_c(int mode, int d);
 
 }  // namespace vg

@@ -19,7 +19,8 @@ const RegEntry *find_reg_a(int mode, int d) {
 // the lookup vesper_search.cu uses
 const RegEntry *find_reg(int mode, int d) {
     const RegEntry *e = find_reg_a(mode, d);
-    return e ? e : find_reg_b(mode, d);
+    if (!e) e = find_reg_b(mode, d);
+    return e ? e : find_reg_c(mode, d);
 }
 
 }  // namespace vg
