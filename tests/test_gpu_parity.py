@@ -363,3 +363,45 @@ def test_fused_scalar_modes_vs_oracle(dev, mode, d):
     mism = np.nonzero(ln[:, 0].cpu().numpy() != lin_ref)[0]
     # Overlap scores are integer counts: translations may tie exactly
     assert len(mism) <= (len(angles) if mode == "O" else 1)
+
+
+def _prob_fields(rng, d):
+    data, vec = small_field(rng, d, zero_frac=0.6)
+    probs = rng.dirichlet([0.5] * 4, size=(d, d, d)).astype(np.float32).transpose(3, 0, 1, 2).copy()
+    probs[:, data == 0] = 0
+    return data, vec, probs
+
+
+@pytest.mark.parametrize("d", [30, 32, 64])
+def test_prob_side64_fp32_paths_vs_fp64_oracle(dev, d):
+    """Prob mode on the register-pass sides (64: grids padded to 64^3): the
+    register passes and the radix-stage passes (float32 FFT) against the
+    oracle in float64, vector and probability scores (1e-4 relative) and the
+    mixed score (1e-3)."""
+    vg = _vg()
+    rng = np.random.default_rng(d)
+    tdata, tvec, tprobs = _prob_fields(rng, d)
+    qdata, qvec, qprobs = _prob_fields(rng, d)
+    angles = orc.calc_angle_comb(30.0)[::173]
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), "prob", 0.0, probs=dev.to_dev(tprobs),
+                                    dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(angles))
+    qd, qv, qp = dev.to_dev(qdata), dev.to_dev(qvec), dev.to_dev(qprobs)
+    tspec = orc.target_spectra([tvec[..., 0], tvec[..., 1], tvec[..., 2]] + list(tprobs))
+    ref = [orc.rot_and_search_prob(tspec, qdata, qvec, list(qprobs), a, 0.5, None, fp64=True) for a in angles]
+    rv = np.array([r[0] for r in ref])
+    rp = np.array([r[2] for r in ref])
+    rd3 = 1.0 / d ** 3
+    st = orc.prob_stats(rv, rp, rd3)
+    mix = (0.5,) + tuple(st)
+    refm = np.array([orc.rot_and_search_prob(tspec, qdata, qvec, list(qprobs), a, 0.5, st, fp64=True)[4]
+                     for a in angles], np.float64)
+    assert vg.search_plan(d, "prob", dev=dev)[0] == 1
+    for path in (0, 1):
+        s1, _ = vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, dev=dev, opts=(path, 0, 0))
+        s2, _ = vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, mix=mix, dev=dev, opts=(path, 0, 0))
+        s1 = s1.cpu().numpy().astype(np.float64)
+        s2 = s2.cpu().numpy().astype(np.float64)
+        assert np.max(np.abs(s1[:, 0] - rv)) / np.max(np.abs(rv)) < 1e-4, path
+        assert np.max(np.abs(s1[:, 1] - rp)) / np.max(np.abs(rp)) < 1e-4, path
+        assert np.max(np.abs(s2[:, 2] - refm)) / np.max(np.abs(refm)) < 1e-3, path

@@ -6,6 +6,10 @@
   python -m vesper_python_gb300.profile_cases prop
       three learned-proposal scorings (committed weights) of one held-out
       128^3 / 64^3 pair at s = 3 over the 10-degree grid
+  python -m vesper_python_gb300.profile_cases prob<d>
+      prob-mode searches (both passes) of seeded random side-d fields with
+      four probability channels over the 15-degree grid, timed per kernel
+      family
 
 Each run is a few GPU milliseconds, so a capture of one of its launches ends
 in seconds.
@@ -39,6 +43,40 @@ def main(argv=None):
         mats = dev.to_dev(vg.rot_matrices(vg.calc_angle_comb(30.0)[:nrot]))
         for _ in range(3):
             vg.search_device(spec, td, tv, "VecProduct", 0.0, mats, dev=dev, tuned=True)
+    elif what.startswith("prob"):
+        # prob mode: both passes (statistics pass, mixed pass) over the 15-degree
+        # grid on seeded random side-d fields with four probability channels;
+        # prints the device time per rotation of each pass and kernel family
+        d = int(what[4:])
+        rng = np.random.default_rng(d)
+
+        def fields():
+            data = rng.uniform(0.1, 2, size=(d, d, d))
+            data[rng.random((d, d, d)) < 0.6] = 0
+            vec = rng.normal(size=(d, d, d, 3))
+            vec /= np.linalg.norm(vec, axis=-1, keepdims=True)
+            vec[data == 0] = 0
+            probs = rng.dirichlet([0.5] * 4, size=(d, d, d)).astype(np.float32).transpose(3, 0, 1, 2).copy()
+            probs[:, data == 0] = 0
+            return dev.to_dev(data), dev.to_dev(vec.astype(np.float32)), dev.to_dev(probs)
+        td, tv, tp = fields()
+        qd, qv, qp = fields()
+        spec = vg.target_spectra_device(td, tv, "prob", 0.0, probs=tp, dev=dev)
+        mats = vg.rot_matrices_device(vg.calc_angle_comb(15.0), dev, key=("grid", 15.0))
+        n = int(mats.shape[0])
+        mix = (0.5, 1.0, 0.0, 1.0, 0.0)
+        for path in ([0, 1] if vg.search_plan(d, "prob", dev=dev)[0] == 1 else [0]):
+            for label, mx in (("pass1", None), ("pass2", mix)):
+                vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, mix=mx, dev=dev, opts=(path, 0, 0))
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(3):
+                    vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, mix=mx, dev=dev, opts=(path, 0, 0))
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / 3
+                print(f"prob side {d} path {path} {label}: {ms:.2f} ms for {n} rotations, "
+                      f"{1000 * ms / n:.3f} us per rotation")
     elif what == "prop":
         net = P.load_weights(dev)[0]
         maker = P.PairMaker(dev)
