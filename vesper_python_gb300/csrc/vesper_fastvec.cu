@@ -41,8 +41,10 @@ struct FvGeom {
     double sorig[3], dorig[3];
 };
 
+// Block (i, a): destination index i on axis a; its threads share the band
+// entries k (the exponentials), each computing the same position and band.
 __global__ void k_fv_tables(const FvGeom g, AxisTables t) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x;
     const int a = blockIdx.y;
     if (i >= g.d) return;
     // (xyz_arr * dest_xwidth + dest_orig - src_orig) / src_xwidth
@@ -51,16 +53,18 @@ __global__ void k_fv_tables(const FvGeom g, AxisTables t) {
     p = __dsub_rn(p, g.sorig[a]);
     p = __ddiv_rn(p, g.sw);
     const int o = a * g.d + i;
-    t.pos[o] = p;
-    t.idx[o] = (p >= 0.0 && p < (double)g.S[a]) ? (int)p : -1;
     int stp = __double2int_rz(__dsub_rn(p, g.fmaxd));
     if (stp < 0) stp = 0;
     int endp = __double2int_rz(__dadd_rn(__dadd_rn(p, g.fmaxd), 1.0));
     if (endp >= g.S[a]) endp = g.S[a];
     const int len = max(0, min(endp - stp, g.WB));
-    t.stp[o] = stp;
-    t.len[o] = len;
-    for (int k = 0; k < g.WB; ++k) {
+    if (threadIdx.x == 0) {
+        t.pos[o] = p;
+        t.idx[o] = (p >= 0.0 && p < (double)g.S[a]) ? (int)p : -1;
+        t.stp[o] = stp;
+        t.len[o] = len;
+    }
+    for (int k = threadIdx.x; k < g.WB; k += blockDim.x) {
         double w = 0.0;
         if (k < len) {
             double r = __dsub_rn((double)(stp + k), p);
@@ -126,13 +130,29 @@ __global__ void __launch_bounds__(256) k_fv_y(const FvGeom g, const AxisTables t
     const int zn = min(kZT, d - z0);
     double *a0 = (double *)smem;
     double *a1 = a0 + (size_t)S1 * kZT;
+    __shared__ int any;   // the tile holds a non-zero partial sum (planes outside the map hold none)
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
     for (int e = threadIdx.x; e < S1 * kZT; e += blockDim.x) {
         const int yp = e / kZT, zz = e - yp * kZT;
         const size_t gi = ((size_t)xp * S1 + yp) * d + z0 + zz;
-        a0[e] = zz < zn ? A0[gi] : 0.0;
-        a1[e] = zz < zn ? A1[gi] : 0.0;
+        const double v0 = zz < zn ? A0[gi] : 0.0, v1 = zz < zn ? A1[gi] : 0.0;
+        a0[e] = v0;
+        a1[e] = v1;
+        if (v0 != 0.0 || v1 != 0.0) any = 1;
     }
     __syncthreads();
+    if (!any) {   // every sum is +0.0, as the loop below would give (A0, A1 >= +0.0)
+        for (int o = threadIdx.x; o < d * kZT; o += blockDim.x) {
+            const int y = o / kZT, zz = o - y * kZT;
+            if (zz >= zn) continue;
+            const size_t go = ((size_t)xp * d + y) * d + z0 + zz;
+            B0[go] = 0.0;
+            B1[go] = 0.0;
+            B2[go] = 0.0;
+        }
+        return;
+    }
     const int *stp = t.stp + d, *len = t.len + d;
     const double *w = t.w + (size_t)g.WB * d, *wp = t.wp + (size_t)g.WB * d;
     for (int o = threadIdx.x; o < d * kZT; o += blockDim.x) {
@@ -298,7 +318,7 @@ extern "C" int vesper_fastvec(const float *src, int sx, int sy, int sz, double s
     if (!workspace || workspace_bytes < need)
         return fail(VESPER_ERR_WORKSPACE, "vesper_fastvec: workspace %zu < %zu bytes", workspace_bytes, need);
     cudaStream_t st = (cudaStream_t)stream;
-    k_fv_tables<<<dim3((dim + 127) / 128, 3), 128, 0, st>>>(g, t);
+    k_fv_tables<<<dim3(dim, 3), 128, 0, st>>>(g, t);
     VG_CHECK_LAUNCH("k_fv_tables");
     const size_t nrows = (size_t)sx * sy;
     const size_t s1 = (size_t)kRB * sz * sizeof(float);
