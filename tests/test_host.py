@@ -152,3 +152,33 @@ def test_workload_generator_is_deterministic():
     assert p.prob1.shape == (32, 32, 32, 4)
     s = p.prob1.sum(-1)
     assert np.allclose(s[p.map1 >= 0.1], 1.0, atol=1e-5) and np.all(s[p.map1 < 0.1] == 0)
+
+
+def test_refine_angle_list_equals_oracle_loop():
+    """The vectorised refinement set equals the reference-order loop (oracle)."""
+    from vesper_python_gb300 import vesper as vg
+    rng = np.random.default_rng(3)
+    for A in (10.0, 15.0, 30.0):
+        grid = vg.calc_angle_comb(A)
+        for _ in range(50):
+            tops = [grid[i] for i in rng.choice(len(grid), 10, replace=False)]
+            a = vg.refine_angle_list(tops)
+            b = orc.refine_angles(tops)
+            assert a.dtype == b.dtype and np.array_equal(a, b)
+
+
+def test_lattice_rows_equal_rot_matrices():
+    """Rows of the 5-degree lattice table are the rotation matrices of the
+    refinement angles bit for bit; off-lattice angles are refused."""
+    from vesper_python_gb300 import vesper as vg
+    rng = np.random.default_rng(4)
+    grid = vg.calc_angle_comb(15.0)
+    tops = [grid[i] for i in rng.choice(len(grid), 10, replace=False)]
+    ref = vg.refine_angle_list(tops)
+    idx = vg.lattice_index(ref)
+    k = np.arange(vg.LATTICE_N) * vg.LATTICE_STEP
+    lat = np.stack(np.meshgrid(k, k, k, indexing="ij"), -1).reshape(-1, 3)
+    assert np.array_equal(lat[idx], ref)
+    assert np.array_equal(vg.rot_matrices(lat[idx]), vg.rot_matrices(ref))
+    assert vg.lattice_index(np.array([[7.0, 0.0, 0.0]])) is None
+    assert vg.lattice_index(np.array([[360.0, 0.0, 0.0]])) is None

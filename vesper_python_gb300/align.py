@@ -239,7 +239,7 @@ class Aligner:
             # ---- 4. refinement around the pair's top-N ----------------------------
             if p.A > 5.0:
                 st.ref_angles = vg.refine_angle_list([angle_comb[r] for r in st.top_h])
-                rmats = dev.to_dev_async(vg.rot_matrices(st.ref_angles))
+                rmats = vg.rot_matrices_lattice(st.ref_angles, dev)
                 st.rs, st.rl = vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats, batch=p.batch,
                                                 dev=dev, tuned=True)
                 st.launches += self._search_launches(st.dim, mode, len(st.ref_angles), p.batch)
@@ -262,7 +262,7 @@ class Aligner:
             if not st.entries:
                 continue
             dim = st.dim
-            sel = dev.to_dev_async(vg.rot_matrices(st.sel_angles))
+            sel = vg.rot_matrices_lattice(st.sel_angles, dev)
             gd, gv, _ = vg.rot_gather_device(st.qdata, st.qvec, sel, dev=dev)
             nm_ = len(st.entries)
             st.res = torch.empty((nm_, 8), dtype=torch.float64, device=dev.device)
@@ -282,13 +282,19 @@ class Aligner:
                 e.record()
                 self.pair_events.append(e)
         resh = self._fetch([[st.res] if st.entries else [] for st in P])
+        # every model's rotation in one scipy call (indexing it gives the
+        # per-angle object exactly)
+        all_ang = [ang for st in P for (ang, _, _) in (st.entries or [])]
+        rots = vg.euler2rot(np.array(all_ang, np.float64)) if all_ang else None
+        ri = 0
         out = []
         for i, st in enumerate(P):
             models = []
             if st.entries:
                 rh = resh[i][0]
                 for k, (ang, sc, tr) in enumerate(st.entries):
-                    r = vg.euler2rot(ang)
+                    r = rots[ri]
+                    ri += 1
                     new_trans = vg.convert_trans(st.c1, st.c2, r, tr, p.s, st.dim)
                     nm, total = rh[k, 0], rh[k, 1]
                     models.append(Model(ang, sc, tr, new_trans, float(nm / total), float(rh[k, 2]), float(rh[k, 3]),

@@ -306,17 +306,58 @@ def rot_matrices_device(angles, dev, key=None):
     return t
 
 
+_REFINE_OFFSETS = np.array(np.meshgrid([-5, 0, 5], [-5, 0, 5], [-5, 0, 5])).T.reshape(-1, 3)
+
+
 def refine_angle_list(sorted_topN_angles):
-    """VESPER_1_prob_new.py:693-713."""
-    refine_ang_list = []
-    for ang in sorted_topN_angles:
-        ang_list = np.array(np.meshgrid([ang[0] - 5, ang[0], ang[0] + 5],
-                                        [ang[1] - 5, ang[1], ang[1] + 5],
-                                        [ang[2] - 5, ang[2], ang[2] + 5])).T.reshape(-1, 3)
-        ang_list = ang_list[(ang_list[:, 0] < 360) & (ang_list[:, 1] < 360) & (ang_list[:, 2] < 180)]
-        ang_list[ang_list < 0] += 360
-        refine_ang_list.append(ang_list)
-    return np.concatenate(refine_ang_list, axis=0)
+    """VESPER_1_prob_new.py:693-713, vectorised: per top angle the 27
+    offsets of +-5 degrees in the reference's meshgrid order, filtered and
+    wrapped as there, concatenated in the same order."""
+    tops = np.asarray(sorted_topN_angles, dtype=np.float64).reshape(-1, 3)
+    cand = (tops[:, None, :] + _REFINE_OFFSETS[None, :, :]).reshape(-1, 3)
+    cand = cand[(cand[:, 0] < 360) & (cand[:, 1] < 360) & (cand[:, 2] < 180)]
+    cand[cand < 0] += 360
+    return cand
+
+
+_LATTICE = {}
+LATTICE_STEP = 5.0
+LATTICE_N = 72
+
+
+def lattice_rot_matrices_device(dev):
+    """rot_matrices of every angle of the 5-degree lattice [0, 360)^3
+    (373,248 rotations, 13 MB), computed once per device.  The angle grids
+    with steps that are multiples of 5 degrees and their +-5 degree
+    refinement sets all lie on it, so their matrices are rows of this table
+    (scipy's vectorised result is row-for-row the per-angle result)."""
+    m = _LATTICE.get(dev.device)
+    if m is None:
+        k = np.arange(LATTICE_N) * LATTICE_STEP
+        lat = np.stack(np.meshgrid(k, k, k, indexing="ij"), -1).reshape(-1, 3)
+        m = _LATTICE[dev.device] = dev.to_dev(rot_matrices(lat))
+    return m
+
+
+def lattice_index(angles):
+    """Row of each angle in the 5-degree lattice, or None when an angle is
+    off the lattice."""
+    a = np.asarray(angles, dtype=np.float64).reshape(-1, 3)
+    q = a / LATTICE_STEP
+    k = np.rint(q)
+    if not (np.all(q == k) and np.all((k >= 0) & (k < LATTICE_N))):
+        return None
+    k = k.astype(np.int64)
+    return (k[:, 0] * LATTICE_N + k[:, 1]) * LATTICE_N + k[:, 2]
+
+
+def rot_matrices_lattice(angles, dev):
+    """Device rot_matrices(angles): rows of the lattice table when the angles
+    are on it (a small index copy), else computed and copied."""
+    idx = lattice_index(angles)
+    if idx is None:
+        return dev.to_dev_async(rot_matrices(angles))
+    return lattice_rot_matrices_device(dev).index_select(0, dev.to_dev_async(idx))
 
 
 def _dev_fields(m, dev):
