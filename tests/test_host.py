@@ -182,3 +182,14 @@ def test_lattice_rows_equal_rot_matrices():
     assert np.array_equal(vg.rot_matrices(lat[idx]), vg.rot_matrices(ref))
     assert vg.lattice_index(np.array([[7.0, 0.0, 0.0]])) is None
     assert vg.lattice_index(np.array([[360.0, 0.0, 0.0]])) is None
+
+
+def test_model_translation_is_convert_trans():
+    """Model.translation (computed on first use) is convert_trans of its
+    angle and translation, as the reference prints it."""
+    from vesper_python_gb300 import align
+    m = align.Model((30.0, 60.0, 90.0), 1.0, (3, 20, 1), 0.5, 0.1, 0.2, 3.0,
+                    (np.array([10.0, 20.0, 30.0]), np.array([5.0, 6.0, 7.0]), 3.0, 24))
+    want = orc.convert_trans(np.array([10.0, 20.0, 30.0]), np.array([5.0, 6.0, 7.0]),
+                             orc.euler2rot((30.0, 60.0, 90.0)), (3, 20, 1), 3.0, 24)
+    assert np.array_equal(m.translation, want)

@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import ctypes
 import dataclasses
+import functools
 
 import numpy as np
 import torch
@@ -52,11 +53,18 @@ class Model:
     angle: tuple
     vec_score: float
     vec_trans: tuple
-    translation: np.ndarray      # converted translation (A), as printed
     overlap: float
     cc: float
     pcc: float
     dot_score: float             # float64 "Score=" of get_score
+    geom: tuple = dataclasses.field(default=None, repr=False)   # (centre 1, centre 2, voxel spacing, side)
+
+    @functools.cached_property
+    def translation(self) -> np.ndarray:
+        """The converted translation (A) as main.py prints it (convert_trans,
+        VESPER_1_prob_new.py:1554-1566), computed when first asked for."""
+        c1, c2, s, dim = self.geom
+        return vg.convert_trans(c1, c2, vg.euler2rot(self.angle), self.vec_trans, s, dim)
 
 
 @dataclasses.dataclass
@@ -282,23 +290,15 @@ class Aligner:
                 e.record()
                 self.pair_events.append(e)
         resh = self._fetch([[st.res] if st.entries else [] for st in P])
-        # every model's rotation in one scipy call (indexing it gives the
-        # per-angle object exactly)
-        all_ang = [ang for st in P for (ang, _, _) in (st.entries or [])]
-        rots = vg.euler2rot(np.array(all_ang, np.float64)) if all_ang else None
-        ri = 0
         out = []
         for i, st in enumerate(P):
             models = []
             if st.entries:
                 rh = resh[i][0]
                 for k, (ang, sc, tr) in enumerate(st.entries):
-                    r = rots[ri]
-                    ri += 1
-                    new_trans = vg.convert_trans(st.c1, st.c2, r, tr, p.s, st.dim)
                     nm, total = rh[k, 0], rh[k, 1]
-                    models.append(Model(ang, sc, tr, new_trans, float(nm / total), float(rh[k, 2]), float(rh[k, 3]),
-                                        float(rh[k, 4])))
+                    models.append(Model(ang, sc, tr, float(nm / total), float(rh[k, 2]), float(rh[k, 3]),
+                                        float(rh[k, 4]), (st.c1, st.c2, p.s, st.dim)))
             self.launches += st.launches
             out.append(AlignResult(st.dim, st.std_s, st.ave_s, st.top_list, models, st.launches))
         self._mark("end")
