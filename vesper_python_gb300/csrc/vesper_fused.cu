@@ -47,8 +47,17 @@ struct FusedArgs {
     unsigned long long *keys;
 };
 
+// CTAs per SM the register budget is sized for, as many as the side's shared
+// volume allows without spilling: 4 (64 registers) up to side 13, 3 up to
+// 15, 2 for 16 to 20, 1 above and for the Laplacian mode (its float64
+// stencil needs the registers).
+template <int MODE, int D>
+constexpr int fused_ctas() {
+    return MODE == VESPER_MODE_LAPLACIAN ? 1 : D <= 13 ? 4 : D <= 15 ? 3 : D <= 20 ? 2 : 1;
+}
+
 template <int MODE, int NCH, int D>
-__global__ void __launch_bounds__(kFusedThreads) k_fused(const FusedArgs a) {
+__global__ void __launch_bounds__(kFusedThreads, fused_ctas<MODE, D>()) k_fused(const FusedArgs a) {
     using G = FGeom<D>;
     constexpr int H = G::H, NP = G::NP, Hp = G::Hp, RS = G::RS, CS = G::CS;
     extern __shared__ __align__(16) unsigned char smem[];

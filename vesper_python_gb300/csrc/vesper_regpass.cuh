@@ -49,8 +49,15 @@ __host__ __device__ inline size_t smem_rc(int ngrp) {
 }
 
 // ---------------------------------------------------------------------------
+// Resident CTAs per SM the register budget is sized for: 4 (64 registers)
+// where the side's pass A fits without spills, 3 (80) for side 75 and prob.
+template <int MODE, int N1, int N2>
+constexpr int rpass_a_ctas() {
+    return (N1 * N2 > 64 || MODE == VESPER_MODE_PROB) ? 3 : 4;
+}
+
 template <int MODE, int NCH, int N1, int N2>
-__global__ void __launch_bounds__(256, 3) k_rpass_a(const PassA2 a) {
+__global__ void __launch_bounds__(256, rpass_a_ctas<MODE, N1, N2>()) k_rpass_a(const PassA2 a) {
     using G = RGeom<N1, N2>;
     constexpr int D = G::D, H = G::H, NP = G::NP, Hp = G::Hp;
     constexpr int PS = 2 * NP * Hp;   // plane stride per channel
