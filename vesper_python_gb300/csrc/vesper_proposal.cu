@@ -542,38 +542,64 @@ __global__ void k_adam(float *w, float *m, float *v, const float *g, int n, floa
 }
 
 // ---- top-k subset: indices of the k largest scores (ties to lower index) --------
-// One block: bisection on the order-preserving bit pattern for the k-th
-// largest value, then an ordered compaction.  The keys sit in shared memory
-// when they fit (skeys), else they are re-read from global memory each round.
+// One block: the k-th largest order-preserving key by a most-significant-digit
+// radix select (four passes of 8 bits over per-warp shared histograms), then
+// an ordered compaction.  The keys sit in shared memory when they fit
+// (skeys), else they are re-read from global memory each pass.
+constexpr int kTkWarps = 1024 / 32;
 __global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int k, int32_t *idx, int skeys) {
-    extern __shared__ uint32_t keys[];
+    extern __shared__ uint32_t dyn[];
+    uint32_t *hist = dyn;                       // [kTkWarps][256] per-warp digit counts
+    uint32_t *keys = dyn + kTkWarps * 256;      // [n] when skeys
     __shared__ unsigned int cnt;
     __shared__ int ncount[1024 / 32];
+    __shared__ uint32_t sel_digit, sel_need;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (skeys) {
         for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = float_order(s[i]);
-        __syncthreads();
     }
+    __syncthreads();
     auto key = [&](int i) -> uint32_t { return skeys ? keys[i] : float_order(s[i]); };
-    uint32_t lo = 0u, hi = 0xffffffffu;   // answer in [lo, hi]: count(key >= t) >= k
-    // the interval halves every round (midpoint taken in 64 bits), so 32
-    // rounds reach lo == hi; the bound is explicit all the same
-    for (int round = 0; round < 40 && lo < hi; ++round) {
-        const uint32_t mid = (uint32_t)(((uint64_t)lo + (uint64_t)hi + 1ull) >> 1);
-        if (threadIdx.x == 0) cnt = 0u;
+    // digits from the top: prefix/mask select the keys that still compete;
+    // need = how many of the k still have to come from them
+    uint32_t prefix = 0u, mask = 0u, need = (uint32_t)k;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (int i = threadIdx.x; i < kTkWarps * 256; i += blockDim.x) hist[i] = 0u;
         __syncthreads();
-        unsigned int c = 0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) c += key(i) >= mid;
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-        if (lane == 0) atomicAdd(&cnt, c);
+        uint32_t *hw = hist + warp * 256;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const uint32_t kv = key(i);
+            if ((kv & mask) == prefix) atomicAdd(&hw[(kv >> shift) & 255u], 1u);
+        }
         __syncthreads();
-        if (cnt >= (unsigned)k)
-            lo = mid;
-        else
-            hi = mid - 1;
+        // fold the warps' histograms into the first one
+        for (int b = threadIdx.x; b < 256; b += blockDim.x) {
+            uint32_t t = 0;
+            for (int w = 0; w < kTkWarps; ++w) t += hist[w * 256 + b];
+            hist[b] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t cum = 0, d = 0, nd = need;
+            for (int b = 255; b >= 0; --b) {
+                const uint32_t c = hist[b];
+                if (cum + c >= need) {
+                    d = (uint32_t)b;
+                    nd = need - cum;
+                    break;
+                }
+                cum += c;
+            }
+            sel_digit = d;
+            sel_need = nd;
+        }
+        __syncthreads();
+        prefix |= sel_digit << shift;
+        mask |= 255u << shift;
+        need = sel_need;
         __syncthreads();
     }
-    const uint32_t t = lo;
+    const uint32_t t = prefix;   // the k-th largest key: count(key > t) < k <= count(key >= t)
     // strictly above the threshold first, then ties in index order, k in total
     if (threadIdx.x == 0) cnt = 0u;
     __syncthreads();
@@ -824,10 +850,11 @@ extern "C" int vesper_prop_adam(float *w, float *m, float *v, const float *g, in
 
 extern "C" int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void *stream) {
     if (!scores || !idx_out || n < 1 || k < 1 || k > n) return fail(VESPER_ERR_INVALID, "topk_subset: bad args");
+    const size_t hb = (size_t)kTkWarps * 256 * sizeof(uint32_t);
     const size_t kb = (size_t)n * sizeof(uint32_t);
-    const int skeys = kb <= (size_t)smem_limit() - 4096 ? 1 : 0;
-    const size_t sm = skeys ? kb : 0;
-    if (skeys) allow_smem(k_topk_subset, sm);
+    const int skeys = hb + kb <= (size_t)smem_limit() - 4096 ? 1 : 0;
+    const size_t sm = hb + (skeys ? kb : 0);
+    allow_smem(k_topk_subset, sm);
     k_topk_subset<<<1, 1024, sm, (cudaStream_t)stream>>>(scores, n, k, idx_out, skeys);
     VG_CHECK_LAUNCH("k_topk_subset");
     return VESPER_OK;
