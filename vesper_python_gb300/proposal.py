@@ -7,7 +7,7 @@ feature field.  A rotation is scored by correlating the target's features
 with the rotated query's features at zero translation (the reference's
 nearest-voxel rotation of the grid).  The top fraction of the angle grid by
 that score is then correlated exactly by vesper_search; the exhaustive search
-remains the fallback and the judge of recall.
+remains the fallback and the measure of recall.
 
 Training labels come from the exhaustive GPU search itself: for each training
 pair the per-rotation best scores are turned into a target distribution

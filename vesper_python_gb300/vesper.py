@@ -612,7 +612,7 @@ def _out_folder(folder):
 
 
 # ----------------------------------------------------------------------------
-# search drivers
+# search entry points
 # ----------------------------------------------------------------------------
 
 def search_map_fft(mrc_target, mrc_search, TopN=10, ang=30, mode="VecProduct", is_eval_mode=False, save_path=".",
