@@ -13,7 +13,10 @@ step aligns a batch of held-out pairs (seeds outside the training range).
 The same pairs are also aligned with the exhaustive search: the line reports
 both rates and the fraction of pairs whose top-1 rotation the two forms
 agree on.  A step runs ``Aligner.align_many`` over its pairs: every stage is
-launched for all pairs before the host waits.  ``--workload pair200_s2_a10``:
+launched for all pairs before the host waits.  The line also reports the
+rate with the global stage (fastVEC, spectra, proposal, global search of
+every pair) replayed as one CUDA graph (``graph_replay``; ``--graph`` makes
+that the headline).  ``--workload pair200_s2_a10``:
 one 200^3 / 100^3 pair per step, exhaustive search (no network).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
@@ -61,6 +64,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--no-exhaustive", action="store_true",
                     help="skip the exhaustive form on the same pairs (profiling runs)")
+    ap.add_argument("--graph", action="store_true",
+                    help="headline value with the global stage replayed as one CUDA graph")
     return ap.parse_args()
 
 
@@ -206,9 +211,11 @@ def run_gb300(args):
     dev_items = [(m1, m2, wd, wd, o1, o2) for (m1, m2, _, _, o1, o2, wd) in pairs]
     host_items = [(h1, h2, wd, wd, o1, o2) for (_, _, h1, h2, o1, o2, wd) in pairs]
 
+    graph = False
+
     def step(params):
         flush.zero_()
-        out = al.align_many(dev_items, params)
+        out = al.align_many(dev_items, params, graph=graph)
         return out, al.launches
 
     def timed(params):
@@ -229,9 +236,16 @@ def run_gb300(args):
         barrier()
         return maxr(e0.elapsed_time(e1)), res, launches, clk.stop()
 
+    # the same steps with the global stage replayed as one CUDA graph (captured
+    # in the warm-up for this batch's shapes and geometry; a batch of new maps
+    # with another grid geometry captures again)
+    graph = True
+    ms_g, _, _, _ = timed(p)
+    graph = bool(args.graph)
     ms, res, launches, clocks = timed(p)
     npairs = len(pairs)
     value = world * npairs * args.steps / (ms / 1e3)
+    value_graph = world * npairs * args.steps / (ms_g / 1e3)
     fallbacks = 0
     if use_prop:
         # fallbacks in one step of the proposal form
@@ -239,13 +253,13 @@ def run_gb300(args):
         fallbacks = sum(al.proposal_info["fallback"])
     # ---- per-stage and per-pass device time: one more step with events ------
     stages = {}
-    al.stages = stages       # stage boundaries only: events between stages
-    step(p)
+    al.stages = stages       # stage boundaries only: events between stages (eager launches)
+    al.align_many(dev_items, p)
     barrier()
     al.stages = None
     prof = {}
     al.profile = prof        # events around every search launch (slower; its own step)
-    step(p)
+    al.align_many(dev_items, p)
     barrier()
     al.profile = None
     # ---- end to end: host maps copied in every step -------------------------
@@ -330,7 +344,10 @@ def run_gb300(args):
         "data": data,
         "config": {"workload": wl, "grid_side": dim, "pairs_per_step": npairs,
                    "rotations": len(vg.calc_angle_comb(p.A)),
-                   "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{world}"},
+                   "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{world}",
+                   "global_stage": "one CUDA graph replay per step" if args.graph else "eager launches"},
+        "graph_replay": {"value": round(value_graph, 4), "unit": UNIT, "ms_per_step": round(ms_g / args.steps, 3),
+                         "note": "global stage as one CUDA graph, captured once for this batch's shapes"},
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": int(launches),
