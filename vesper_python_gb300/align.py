@@ -244,10 +244,17 @@ class Aligner:
             st.top_list = [(tuple(angle_comb[r]), float(score_grid[r]), vg.unravel(lin_grid[r], st.dim))
                            for r in top_h]
             st.top_h = top_h
-            # ---- 4. refinement around the pair's top-N ----------------------------
-            if p.A > 5.0:
-                st.ref_angles = vg.refine_angle_list([angle_comb[r] for r in st.top_h])
-                rmats = vg.rot_matrices_lattice(st.ref_angles, dev)
+        # ---- 4. refinement around each pair's top-N: every pair's angle set and
+        # matrices at once (one index copy and one gather from the lattice
+        # table), then the searches
+        if p.A > 5.0:
+            sets = [vg.refine_angle_list([angle_comb[r] for r in st.top_h]) for st in P]
+            allm = vg.rot_matrices_lattice(np.concatenate(sets), dev)
+            off = 0
+            for st, ra in zip(P, sets):
+                st.ref_angles = ra
+                rmats = allm[off:off + len(ra)]
+                off += len(ra)
                 st.rs, st.rl = vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats, batch=p.batch,
                                                 dev=dev, tuned=True)
                 st.launches += self._search_launches(st.dim, mode, len(st.ref_angles), p.batch)
@@ -267,18 +274,27 @@ class Aligner:
             else:
                 st.sel_angles = np.array([e[0] for e in st.top_list])
                 st.entries = st.top_list
+        # every pair's model matrices and wrapped translations in one copy each
+        # (translations wrapped to (-d/2, d/2] as get_score does, :1323-1329)
+        withm = [st for st in P if st.entries]
+        if withm:
+            selm = vg.rot_matrices_lattice(np.concatenate([np.asarray(st.sel_angles, np.float64).reshape(-1, 3)
+                                                           for st in withm]), dev)
+            trd_all = dev.to_dev_async(np.array([[t - st.dim if t > 0.5 * st.dim else t for t in tr]
+                                                 for st in withm for (_, _, tr) in st.entries], np.int32))
+        off = 0
+        for i, st in enumerate(P):
             if not st.entries:
                 continue
             dim = st.dim
-            sel = vg.rot_matrices_lattice(st.sel_angles, dev)
-            gd, gv, _ = vg.rot_gather_device(st.qdata, st.qvec, sel, dev=dev)
             nm_ = len(st.entries)
+            sel = selm[off:off + nm_]
+            trd = trd_all[off:off + nm_]
+            off += nm_
+            gd, gv, _ = vg.rot_gather_device(st.qdata, st.qvec, sel, dev=dev)
             st.res = torch.empty((nm_, 8), dtype=torch.float64, device=dev.device)
-            # translations wrapped to (-d/2, d/2] as get_score does (:1323-1329)
-            trw = np.array([[t - dim if t > 0.5 * dim else t for t in tr] for (_, _, tr) in st.entries], np.int32)
-            trd = dev.to_dev_async(trw)
-            ws = torch.empty(_native.size_query("vesper_rescore_batch_workspace_size", dim, nm_), dtype=torch.uint8,
-                             device=dev.device)
+            ws = dev.workspace(("rescore_batch", i, dim, nm_),
+                               _native.size_query("vesper_rescore_batch_workspace_size", dim, nm_))
             _native.check(self.lib.vesper_rescore_batch(
                 ctypes.c_void_p(st.tdata.data_ptr()), ctypes.c_void_p(st.tvec.data_ptr()), float(sh[i, 2]),
                 float(sh[i, 3]), float(sh[i, 4]), ctypes.c_void_p(gd.data_ptr()), ctypes.c_void_p(gv.data_ptr()),

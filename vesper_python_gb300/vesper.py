@@ -420,6 +420,10 @@ def target_spectra_device(data, vec, mode, ave, probs=None, dev=None):
     return spec
 
 
+_TUNED = {}          # (device, side, mode) -> the autotuner's launch shape
+_SEARCH_SIZES = {}   # (side, mode, mixed, batch, rotations) -> (scores per rotation, workspace bytes)
+
+
 def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, batch=0, dev=None, profile=None,
                   opts=None, tuned=False):
     """vesper_search: (scores f32 [n][nscore], lin int32 [n][nscore]) CUDA tensors.
@@ -430,14 +434,22 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
     code = mode if isinstance(mode, int) else MODE_CODES[mode]
     n = int(rotmats.shape[0])
     if tuned and opts is None and batch == 0 and not isinstance(mode, int):
-        from . import autotune
-        t = autotune.tune(dev, spec, data, vec, mode, ave, rotmats, probs=probs, mix=mix)
+        tk = (dev.device, d, mode)
+        t = _TUNED.get(tk)
+        if t is None:
+            from . import autotune
+            t = autotune.tune(dev, spec, data, vec, mode, ave, rotmats, probs=probs, mix=mix)
+            _TUNED[tk] = t
         batch = int(t["batch"])
         opts = (-1, int(t["cchunk"]), int(t["W"]))
-    nscore = dev.lib.vesper_search_nscore(code, 1 if mix is not None else 0)
+    sk = (d, code, mix is not None, int(batch), max(n, 1))
+    sz = _SEARCH_SIZES.get(sk)
+    if sz is None:
+        sz = _SEARCH_SIZES[sk] = (dev.lib.vesper_search_nscore(code, 1 if mix is not None else 0),
+                                  _native.size_query("vesper_search_workspace_size", d, code, int(batch), max(n, 1)))
+    nscore, ws_bytes = sz
     scores = torch.empty((n, nscore), dtype=torch.float32, device=dev.device)
     lin = torch.empty((n, nscore), dtype=torch.int32, device=dev.device)
-    ws_bytes = _native.size_query("vesper_search_workspace_size", d, code, int(batch), max(n, 1))
     ws = dev.workspace(("search", d, code, int(batch)), ws_bytes)
     mixarr = (ctypes.c_double * 5)(*[float(v) for v in mix]) if mix is not None else None
     args = (_ptr(spec), _ptr(data), _ptr(vec), _ptr(probs), d, code, float(ave or 0.0), _ptr(rotmats), n, mixarr,
@@ -457,16 +469,24 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
     return scores, lin
 
 
+_PLANS = {}
+
+
 def search_plan(dim, mode, batch=0, nrot=1, opts=None, dev=None):
     """vesper_search_plan: (kernel family 0 radix / 1 register / 2 fused,
     kernel launches of one search call)."""
     dev = dev or default_device()
     code = mode if isinstance(mode, int) else MODE_CODES[mode]
+    key = (dev.device, int(dim), code, int(batch), int(nrot), tuple(opts) if opts is not None else None)
+    got = _PLANS.get(key)
+    if got is not None:
+        return got
     path = ctypes.c_int(0)
     nl = ctypes.c_int(0)
     copts = (ctypes.c_int * 3)(*[int(v) for v in opts]) if opts is not None else None
     _native.check(dev.lib.vesper_search_plan(int(dim), code, int(batch), int(nrot), copts, ctypes.byref(path),
                                              ctypes.byref(nl)))
+    _PLANS[key] = (path.value, nl.value)
     return path.value, nl.value
 
 
