@@ -66,6 +66,8 @@ def parse():
                     help="skip the exhaustive form on the same pairs (profiling runs)")
     ap.add_argument("--graph", action="store_true",
                     help="headline value with the global stage replayed as one CUDA graph")
+    ap.add_argument("--no-graph-replay", action="store_true",
+                    help="skip the CUDA-graph measurement (profiler launch lists)")
     return ap.parse_args()
 
 
@@ -239,13 +241,15 @@ def run_gb300(args):
     # the same steps with the global stage replayed as one CUDA graph (captured
     # in the warm-up for this batch's shapes and geometry; a batch of new maps
     # with another grid geometry captures again)
-    graph = True
-    ms_g, _, _, _ = timed(p)
+    ms_g = None
+    if not args.no_graph_replay or args.graph:
+        graph = True
+        ms_g, _, _, _ = timed(p)
     graph = bool(args.graph)
     ms, res, launches, clocks = timed(p)
     npairs = len(pairs)
     value = world * npairs * args.steps / (ms / 1e3)
-    value_graph = world * npairs * args.steps / (ms_g / 1e3)
+    value_graph = world * npairs * args.steps / (ms_g / 1e3) if ms_g else None
     fallbacks = 0
     if use_prop:
         # fallbacks in one step of the proposal form
@@ -347,7 +351,8 @@ def run_gb300(args):
                    "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{world}",
                    "global_stage": "one CUDA graph replay per step" if args.graph else "eager launches"},
         "graph_replay": {"value": round(value_graph, 4), "unit": UNIT, "ms_per_step": round(ms_g / args.steps, 3),
-                         "note": "global stage as one CUDA graph, captured once for this batch's shapes"},
+                         "note": "global stage as one CUDA graph, captured once for this batch's shapes"}
+        if value_graph else None,
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": int(launches),
