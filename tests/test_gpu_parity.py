@@ -405,3 +405,50 @@ def test_prob_side64_fp32_paths_vs_fp64_oracle(dev, d):
         assert np.max(np.abs(s1[:, 0] - rv)) / np.max(np.abs(rv)) < 1e-4, path
         assert np.max(np.abs(s1[:, 1] - rp)) / np.max(np.abs(rp)) < 1e-4, path
         assert np.max(np.abs(s2[:, 2] - refm)) / np.max(np.abs(refm)) < 1e-3, path
+
+
+@pytest.mark.parametrize("mode", ["O", "C", "P", "L"])
+def test_register_passes_scalar_modes_side75(dev, mode):
+    """Register passes of the scalar modes at side 75 against the radix-stage
+    passes and the oracle on a few rotations."""
+    vg = _vg()
+    name = orc.MODES[mode]
+    d = 75
+    assert vg.search_plan(d, name, dev=dev)[0] == 1
+    rng = np.random.default_rng(1075)
+    tdata, tvec = small_field(rng, d, zero_frac=0.6)
+    qdata, qvec = small_field(rng, d, zero_frac=0.6)
+    ave = float(np.mean(tdata[tdata > 0]))
+    angles = orc.calc_angle_comb(30.0)[::251]
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), name, ave, dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(angles))
+    out = {}
+    for path in (0, 1):
+        sc, ln = vg.search_device(spec, dev.to_dev(qdata), dev.to_dev(qvec), name, ave, mats, dev=dev,
+                                  opts=(path, 0, 0))
+        out[path] = sc[:, 0].cpu().numpy().astype(np.float64)
+    ts = orc.target_spectra(orc.mode_field(mode, tdata, tvec, ave))
+    osc, _ = orc.search(ts, mode, qdata, qvec, angles, ave)
+    scale = np.max(np.abs(osc))
+    for path in (0, 1):
+        assert np.max(np.abs(out[path] - osc)) <= SCORE_RTOL * scale, path
+
+
+def test_all_zero_query_takes_the_first_translation(dev):
+    """An all-zero rotated query gives an all-zero correlation volume; numpy's
+    argmax (and so the reference) returns translation 0 whatever the signs of
+    the zeros, on every kernel family."""
+    vg = _vg()
+    for d in (13, 30):
+        rng = np.random.default_rng(d)
+        tdata, tvec = small_field(rng, d, zero_frac=0.5)
+        qdata = np.zeros((d, d, d))
+        qvec = np.zeros((d, d, d, 3), np.float32)
+        spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), "VecProduct", 0.0, dev=dev)
+        mats = dev.to_dev(vg.rot_matrices(orc.calc_angle_comb(30.0)[:20]))
+        paths = [0, vg.search_plan(d, "VecProduct", dev=dev)[0]]
+        for path in sorted(set(paths)):
+            sc, ln = vg.search_device(spec, dev.to_dev(qdata), dev.to_dev(qvec), "VecProduct", 0.0, mats, dev=dev,
+                                      opts=(path, 0, 0))
+            assert np.all(sc[:, 0].cpu().numpy() == 0.0), (d, path)
+            assert np.all(ln[:, 0].cpu().numpy() == 0), (d, path)

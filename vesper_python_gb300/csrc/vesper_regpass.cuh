@@ -50,10 +50,11 @@ __host__ __device__ inline size_t smem_rc(int ngrp) {
 
 // ---------------------------------------------------------------------------
 // Resident CTAs per SM the register budget is sized for: 4 (64 registers)
-// where the side's pass A fits without spills, 3 (80) for side 75 and prob.
+// where the side's pass A fits without spills, 3 (80) for side 75 and prob,
+// 2 for the Laplacian mode (its float64 stencil).
 template <int MODE, int N1, int N2>
 constexpr int rpass_a_ctas() {
-    return (N1 * N2 > 64 || MODE == VESPER_MODE_PROB) ? 3 : 4;
+    return MODE == VESPER_MODE_LAPLACIAN ? 2 : (N1 * N2 > 64 || MODE == VESPER_MODE_PROB) ? 3 : 4;
 }
 
 template <int MODE, int NCH, int N1, int N2>
