@@ -244,6 +244,22 @@ int vesper_rescore_batch(const double *tdata, const float *tvec, double tave, do
                          double *result_out, void *workspace, size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Probability-map hole filling (interpolate, interpolation_functions.py:6-135)
+ * in place on a DEVICE float32 [nx][ny][nz][nch] array: the parity of the
+ * first voxel (C order) with channel 0 > 0 fixes the sampled lattice; zero
+ * voxels off it take the float64 mean of their neighbours along the axes
+ * where their parity differs (one axis, then two, then three), rounded to
+ * float32, with the reference's wrap of index -1 and its loop bounds.
+ * workspace: DEVICE, >= 8 bytes.  vesper_prob_interpolate_found (after the
+ * call, synchronising the stream) sets *found = 0 when no voxel had a
+ * positive channel 0, in which case the data is unchanged (the reference
+ * fails there on an unbound variable).
+ * ------------------------------------------------------------------------- */
+int vesper_prob_interpolate(float *data, int nx, int ny, int nz, int nch, void *workspace, size_t workspace_bytes,
+                            void *stream);
+int vesper_prob_interpolate_found(const void *workspace, int *found, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Learned rotation proposal (no counterpart in the reference): a 3-D
  * convolutional encoder over each map's fields and the rotational
  * correlation of the two feature fields at zero translation, which orders

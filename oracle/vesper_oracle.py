@@ -492,3 +492,40 @@ def prob_stats(vscores, pscores, rd3):
     v = np.asarray(vscores, np.float64) * rd3
     p = np.asarray(pscores, np.float64) * rd3
     return np.std(v), np.mean(v), np.std(p), np.mean(p)
+
+
+# --------------------------------------------------------------------------
+# probability-map hole filling (interpolation_functions.py:6-135)
+# --------------------------------------------------------------------------
+
+def interpolate(data):
+    """interpolate, in place on a [X][Y][Z][C] float32 array: the parity of
+    the first voxel (C order) with channel 0 > 0 fixes the reference lattice;
+    zero voxels whose parity differs on one axis (x, y, z), then on two (xy,
+    xz, yz), then on all three take the float64 mean of their neighbours along
+    the differing axes (x pair, y pair, z pair in that order), rounded to
+    float32.  Index -1 wraps to the last element and each axis stops before
+    its last index, as the reference's loops do."""
+    pos = np.argwhere(data[..., 0] > 0)
+    if len(pos) == 0:
+        raise ValueError("interpolate: no voxel with a positive first channel (the reference's ref_x is unbound)")
+    ref = [int(v) % 2 for v in pos[0]]
+    shape = data.shape[:3]
+    for m in (1, 2, 4, 3, 5, 6, 7):
+        start = [(r + 1) % 2 if m & (1 << a) else r for a, r in enumerate(ref)]
+        idx = [np.arange(start[a], shape[a] - 1, 2) for a in range(3)]
+        if any(len(i) == 0 for i in idx):
+            continue
+        cell = data[np.ix_(*idx)]
+        acc = np.zeros(cell.shape, np.float64)
+        n = 0
+        for a in range(3):
+            if m & (1 << a):
+                up = list(idx)
+                dn = list(idx)
+                up[a] = idx[a] + 1
+                dn[a] = idx[a] - 1          # -1 indexes the last element, as in Python
+                acc += data[np.ix_(*up)]
+                acc += data[np.ix_(*dn)]
+                n += 2
+        data[np.ix_(*idx)] = np.where(cell == 0, (acc / n).astype(np.float32), cell)

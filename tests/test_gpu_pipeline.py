@@ -214,3 +214,49 @@ def test_align_many_graph_replay_equals_eager(dev):
             assert [m.angle for m in r.models] == [m.angle for m in a.models]
             assert [m.dot_score for m in r.models] == [m.dot_score for m in a.models]
             assert (r.ave, r.std) == (a.ave, a.std)
+
+
+def test_prob_interpolate_golden_and_oracle(dev, golden_dir):
+    """GPU hole filling against the reference function's outputs (golden) and
+    against the oracle on a larger map, bit for bit; a map without a positive
+    first channel raises as the reference does."""
+    from vesper_python_gb300 import vesper as vg
+    g = np.load(os.path.join(golden_dir, "interp_small.npz"))
+    for n in range(4):
+        a = g[f"in{n}"].copy()
+        vg.interpolate(a)
+        np.testing.assert_array_equal(a, g[f"out{n}"])
+    rng = np.random.default_rng(7)
+    a = np.zeros((61, 70, 83, 4), np.float32)
+    a[1::2, ::2, 1::2] = rng.random(a[1::2, ::2, 1::2].shape).astype(np.float32)
+    a[rng.random(a.shape) < 0.05] = 0.0
+    b = a.copy()
+    orc.interpolate(b)
+    t = dev.to_dev(a)
+    vg.interpolate_device(t, dev)
+    np.testing.assert_array_equal(t.cpu().numpy(), b)
+    with pytest.raises(UnboundLocalError):
+        vg.interpolate(np.zeros((4, 4, 4, 4), np.float32))
+
+
+def test_interpolation_cli(dev, tmp_path, golden_dir):
+    """interpolation.py insert/graph: prints, the saved .npy equals the
+    reference's output, one MRC per channel."""
+    from vesper_python_gb300 import interpolation, mrc
+    g = np.load(os.path.join(golden_dir, "interp_small.npz"))
+    np.save(tmp_path / "in.npy", g["in0"])
+    ref_map = tmp_path / "ref.mrc"
+    mrc.write_mrc(ref_map, np.zeros(g["in0"].shape[2::-1], np.float32), voxel_size=1.0, origin=(1.0, 2.0, 3.0))
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        interpolation.main(["graph", "-f", str(tmp_path / "in.npy"), "-s", str(tmp_path / "out"), "-m", str(ref_map)])
+    lines = buf.getvalue().splitlines()
+    assert lines[0] == "Usage Modes:" and lines[4:8] == [str(v) for v in g["in0"].shape]
+    assert lines[8] == "Saved interpolated map as: " + str(tmp_path / "out") + ".npy"
+    np.testing.assert_array_equal(np.load(tmp_path / "out.npy"), g["out0"])
+    for c in range(4):
+        m = mrc.read_mrc(tmp_path / f"out_{c}.mrc")
+        nx, ny, nz = g["out0"].shape[:3]
+        np.testing.assert_array_equal(m.data[:nz - 2, :ny - 2, :nx - 2],
+                                      np.transpose(g["out0"][:nx - 2, :ny - 2, :nz - 2, c], (2, 1, 0)))
+        assert tuple(m.origin) == (1.0, 2.0, 3.0)

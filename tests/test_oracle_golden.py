@@ -148,3 +148,13 @@ def test_next_fast_len():
         [1, 2, 11, 13, 18, 20, 24, 30, 39, 75, 98, 144, 175]
     # 11*13 and 13*13 need e+f = 2 -> skipped
     assert orc.next_fast_len(143) == 144
+
+
+def test_interpolate_oracle_matches_golden(golden_dir):
+    """The oracle's probability-map hole filling against the reference
+    function's outputs (interpolation_functions.py:6-135), bit for bit."""
+    g = np.load(os.path.join(golden_dir, "interp_small.npz"))
+    for n in range(4):
+        a = g[f"in{n}"].copy()
+        orc.interpolate(a)
+        np.testing.assert_array_equal(a, g[f"out{n}"])

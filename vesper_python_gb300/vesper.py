@@ -816,3 +816,35 @@ def search_map_fft_prob(mrc_P1, mrc_P2, mrc_P3, mrc_P4, mrc_target, mrc_search, 
             show_vec(mrc_target.orig, result_mrc["vec"], result_mrc["data"], sr.sco_arr, result_mrc["mixed_score"],
                      mrc_search.xwidth, result_mrc["mixed_trans"], result_mrc["angle"], folder_path, i)
     return refined_list
+
+
+# ----------------------------------------------------------------------------
+# probability-map hole filling (interpolation_functions.py:6-135)
+# ----------------------------------------------------------------------------
+
+def interpolate_device(data, dev=None):
+    """vesper_prob_interpolate in place on a CUDA float32 [X][Y][Z][C] tensor."""
+    dev = dev or default_device()
+    if data.dtype != torch.float32 or not data.is_contiguous() or data.dim() != 4:
+        raise ValueError("interpolate_device: a contiguous float32 [X][Y][Z][C] CUDA tensor is needed")
+    ws = dev.workspace(("interp",), 8)
+    nx, ny, nz, nc = (int(v) for v in data.shape)
+    _native.check(dev.lib.vesper_prob_interpolate(_ptr(data), nx, ny, nz, nc, _ptr(ws), ws.numel(), dev.stream))
+    found = ctypes.c_int(0)
+    _native.check(dev.lib.vesper_prob_interpolate_found(_ptr(ws), ctypes.byref(found), dev.stream))
+    if not found.value:
+        raise UnboundLocalError("local variable 'ref_x' referenced before assignment")
+    return data
+
+
+def interpolate(data):
+    """interpolation_functions.interpolate on the GPU: fills the zero voxels
+    of the [X][Y][Z][C] probability array in place and returns None, as the
+    reference does."""
+    arr = np.asarray(data)
+    t = torch.as_tensor(np.ascontiguousarray(arr, np.float32)).to(default_device().device)
+    interpolate_device(t)
+    out = t.cpu().numpy()
+    if isinstance(data, np.ndarray):
+        data[...] = out.astype(data.dtype, copy=False)
+    return None
