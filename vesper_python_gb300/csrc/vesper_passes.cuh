@@ -67,7 +67,23 @@ struct PassA2 {
     FftPlan P;
     float2 *S;                    // [batch][nch][d][d][H]
     unsigned long long *keys;     // [nrot][nscore]
+    const double *rd;             // Laplacian mode: [batch][d^3] rotated density, or null
 };
+
+// Pass-A sample of rotation b of the batch: the Laplacian mode reads the
+// batch's gathered density when it is there, every other mode gathers.
+template <int MODE, int NCH>
+__device__ __forceinline__ void sample_a(const PassA2 &a, const float (&F)[9], int b, int x, int y, int z,
+                                         float *out) {
+    if constexpr (MODE == VESPER_MODE_LAPLACIAN) {
+        if (a.rd) {
+            const int d = a.src.d;
+            out[0] = lap_from_rd(a.rd + (size_t)b * d * d * d, d, x, y, z);
+            return;
+        }
+    }
+    sample_fast<MODE>(a.src, F, x, y, z, out);
+}
 
 __host__ __device__ inline size_t smem_a2(int d, int ntab, int cchunk) {
     const PlaneGeom g = plane_geom(d);
@@ -98,9 +114,9 @@ __global__ void __launch_bounds__(512) k_pass_a(const PassA2 a) {
         for (Walk2 w(d); w.o < np; w.next()) {
             const int p = w.o, z = w.i, y0 = 2 * p;
             float v0[NCH], v1[NCH];
-            sample_fast<MODE>(a.src, Fr, x, y0, z, v0);
+            sample_a<MODE, NCH>(a, Fr, b, x, y0, z, v0);
             if (y0 + 1 < d) {
-                sample_fast<MODE>(a.src, Fr, x, y0 + 1, z, v1);
+                sample_a<MODE, NCH>(a, Fr, b, x, y0 + 1, z, v1);
             } else {
 #pragma unroll
                 for (int c = 0; c < NCH; ++c) v1[c] = 0.f;

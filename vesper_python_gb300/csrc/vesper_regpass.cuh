@@ -80,9 +80,9 @@ __global__ void __launch_bounds__(256, rpass_a_ctas<MODE, N1, N2>()) k_rpass_a(c
         for (Walk2 w(D); w.o < NP; w.next()) {
             const int p = w.o, z = w.i, y0 = 2 * p;
             float v0[NCH], v1[NCH];
-            sample_fast<MODE>(a.src, Fr, x, y0, z, v0);
+            sample_a<MODE, NCH>(a, Fr, b, x, y0, z, v0);
             if (y0 + 1 < D) {
-                sample_fast<MODE>(a.src, Fr, x, y0 + 1, z, v1);
+                sample_a<MODE, NCH>(a, Fr, b, x, y0 + 1, z, v1);
             } else {
 #pragma unroll
                 for (int c = 0; c < NCH; ++c) v1[c] = 0.f;

@@ -141,6 +141,25 @@ __device__ __forceinline__ void sample_fast(const Src &s, const float (&F)[9], i
     }
 }
 
+// laplacian_filter of the rotated density at (x, y, z) from that density
+// already gathered into rd[d^3] (k_rot_density): the arithmetic of sample<L>
+// below, with plain reads where sample<L> gathers each of the seven values.
+__device__ __forceinline__ float lap_from_rd(const double *rd, int d, int x, int y, int z) {
+    auto D = [&](int xx, int yy, int zz) -> double { return rd[((size_t)xx * d + yy) * d + zz]; };
+    const double c = D(x, y, z);
+    double acc = 0.0;
+    if (c > 0) {
+        acc = __dmul_rn(-6.0, c);
+        if (x + 1 < d) acc = __dadd_rn(acc, D(x + 1, y, z));
+        if (x - 1 >= 0) acc = __dadd_rn(acc, D(x - 1, y, z));
+        if (y + 1 < d) acc = __dadd_rn(acc, D(x, y + 1, z));
+        if (y - 1 >= 0) acc = __dadd_rn(acc, D(x, y - 1, z));
+        if (z + 1 < d) acc = __dadd_rn(acc, D(x, y, z + 1));
+        if (z - 1 >= 0) acc = __dadd_rn(acc, D(x, y, z - 1));
+    }
+    return (float)acc;
+}
+
 // Channel values of the rotated query at (x, y, z): out[c] for every channel.
 template <int MODE>
 __device__ __forceinline__ void sample(const Src &s, const float *F, int x, int y, int z, float *out) {

@@ -129,6 +129,24 @@ extern "C" int vesper_search_nscore(int mode, int with_mix) {
     return 1;
 }
 
+// Laplacian mode: the rotated density of every rotation of a batch
+// (rot_mrc's gather, density != 0 mask), so that pass A computes the filter
+// from plain reads instead of seven gathers per voxel.
+__global__ void k_rot_density(const Src s, const float *rotmats, int r0, double *rd) {
+    __shared__ float F[9];
+    const int b = blockIdx.y;
+    if (threadIdx.x < 9) F[threadIdx.x] = rotmats[(size_t)(r0 + b) * 9 + threadIdx.x];
+    __syncthreads();
+    const int d = s.d;
+    const size_t n = (size_t)d * d * d;
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const int x = (int)(v / ((size_t)d * d)), y = (int)((v / d) % d), z = (int)(v % d);
+    float4 w;
+    const int i = gather4(F, d, x, y, z, s.q4, w);
+    rd[(size_t)b * n + v] = i >= 0 ? s.data[i] : 0.0;
+}
+
 extern "C" int vesper_search_workspace_size(int dim, int mode, int batch, int nrot, size_t *bytes) {
     if (!bytes) return fail(VESPER_ERR_INVALID, "bytes is NULL");
     if (batch <= 0) batch = default_batch(dim, mode);
@@ -139,6 +157,7 @@ extern "C" int vesper_search_workspace_size(int dim, int mode, int batch, int nr
     cv.take<float2>((size_t)batch * mode_nch(mode) * dim * dim * H);
     cv.take<float2>((size_t)batch * mode_ngrp(mode) * dim * dim * H);
     cv.take<unsigned long long>((size_t)std::max(nrot, 1) * 3);
+    if (mode == VESPER_MODE_LAPLACIAN) cv.take<double>((size_t)batch * N);
     *bytes = cv.off + 256;
     return VESPER_OK;
 }
@@ -213,6 +232,7 @@ static int search_impl(const void *spectra, const double *data, const float *vec
     float2 *S = cv.take<float2>((size_t)batch * nch * dim * dim * H);
     float2 *U = cv.take<float2>((size_t)batch * ngrp * dim * dim * H);
     unsigned long long *keys = cv.take<unsigned long long>((size_t)nrot * 3);
+    double *rd = mode == VESPER_MODE_LAPLACIAN ? cv.take<double>((size_t)batch * N) : nullptr;
 
     switch (mode) {
         case VESPER_MODE_VEC: launch_pack<VESPER_MODE_VEC>(data, vec, probs, dim, ave, q4, p4, st); break;
@@ -233,7 +253,7 @@ static int search_impl(const void *spectra, const double *data, const float *vec
         mx.pstd = (float)mix[3];
         mx.pave = (float)mix[4];
     }
-    PassA2 pa{Src{q4, p4, data, dim}, rotmats, 0, nch, cfg.cchunk, nscore, P, S, keys};
+    PassA2 pa{Src{q4, p4, data, dim}, rotmats, 0, nch, cfg.cchunk, nscore, P, S, keys, rd};
     PassB2 pb{S, (const float2 *)spectra, U, dim, nch, ngrp, mode == VESPER_MODE_PROB ? 3 : nch, cfg.W, P};
     PassC2 pc{U, dim, ngrp, 0, nscore, P, mx, keys};
     allow_smem(k_pass_b, cfg.sb);
@@ -279,6 +299,10 @@ static int search_impl(const void *spectra, const double *data, const float *vec
         pc.r0 = r0;
         const dim3 gplane(dim, nb);
         mark(0, 0);
+        if (rd) {
+            k_rot_density<<<dim3((unsigned)((N + 255) / 256), nb), 256, 0, st>>>(pa.src, rotmats, r0, rd);
+            VG_CHECK_LAUNCH("k_rot_density");
+        }
         if (cfg.path == 1) {
             reg->a(gplane, kThreads, cfg.sa, st, pa);
             VG_CHECK_LAUNCH("k_rpass_a");
@@ -393,7 +417,8 @@ extern "C" int vesper_search_plan(int dim, int mode, int batch, int nrot, const 
     if (batch <= 0) batch = default_batch(dim, mode);
     const int nb = nrot > 0 ? (nrot + batch - 1) / batch : 0;
     *path_out = path;
-    *launches_out = nrot > 0 ? 2 + (path == 2 ? 1 : 3 * nb) : 0;   // pack + passes + decode
+    // pack + passes (+ the gathered density of each Laplacian batch) + decode
+    *launches_out = nrot > 0 ? 2 + (path == 2 ? 1 : (mode == VESPER_MODE_LAPLACIAN ? 4 : 3) * nb) : 0;
     return VESPER_OK;
 }
 
