@@ -3,7 +3,8 @@ reference by tests/golden).  Tolerances:
 
 * gather (rot_mrc / rot_mrc_prob): bit-exact;
 * fastVEC: float64 density within 1e-12 relative; float32 vectors within
-  2e-6 absolute (a few ulp: the GPU sums the separable window in another order);
+  2e-6 absolute (a few ulp: the GPU sums the separable window in another order,
+  in float-float pairs, or in float64 for very narrow windows);
 * search: raw scores within 1e-4 relative to the largest |score| (the
   reference-path FFT is single precision); best translations index-exact
   except where the GPU's pick scores within that tolerance of the oracle's
@@ -131,6 +132,24 @@ def test_fastvec_pair128_maps(dev):
         assert np.array_equal(data != 0, ref_d != 0)
         assert np.max(np.abs(data - ref_d) / np.maximum(np.abs(ref_d), 1e-300)) < 1e-12
         assert np.max(np.abs(vec.cpu().numpy() - ref_v)) < 2e-6
+
+
+def test_fastvec_narrow_window_float64_path(dev):
+    """dreso / src_width = 0.7: the smallest band weight (about 2e-31) is below
+    what a float-float pair holds to full precision, so the contractions run in
+    float64; same tolerances."""
+    vg = _vg()
+    rng = np.random.default_rng(11)
+    src = rng.uniform(0.2, 1.0, size=(20, 18, 16)).astype(np.float32)
+    src[rng.random(src.shape) < 0.4] = 0
+    so, do = np.array([0.5, -0.25, 0.0]), np.array([1.0, 0.75, 0.5])
+    ref_d, ref_v = orc.fastvec(src, 1.0, so, 9, 2.0, do, 0.7)
+    data, _, vec = vg.fastvec_device(src, 1.0, so, 9, 2.0, do, 0.7, dev=dev)
+    data = data.cpu().numpy()
+    assert np.count_nonzero(ref_d) > 100
+    assert np.array_equal(data != 0, ref_d != 0)
+    assert np.max(np.abs(data - ref_d) / np.maximum(np.abs(ref_d), 1e-300)) < 1e-12
+    assert np.max(np.abs(vec.cpu().numpy() - ref_v)) < 2e-6
 
 
 # ---------------------------------------------------------------------------

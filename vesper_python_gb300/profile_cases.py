@@ -6,6 +6,9 @@
   python -m vesper_python_gb300.profile_cases prop
       three learned-proposal scorings (committed weights) of one held-out
       128^3 / 64^3 pair at s = 3 over the 10-degree grid
+  python -m vesper_python_gb300.profile_cases fastvec
+      fastVEC of both maps of the seed-0 128^3 / 64^3 generator pair at s = 3,
+      g = 16 (the learned-proposal workload's maps), timed per map
   python -m vesper_python_gb300.profile_cases prob<d>
       prob-mode searches (both passes) of seeded random side-d fields with
       four probability channels over the 15-degree grid, timed per kernel
@@ -77,6 +80,27 @@ def main(argv=None):
                 ms = e0.elapsed_time(e1) / 3
                 print(f"prob side {d} path {path} {label}: {ms:.2f} ms for {n} rotations, "
                       f"{1000 * ms / n:.3f} us per rotation")
+    elif what == "fastvec":
+        import contextlib
+        import io
+
+        from . import synth
+        pair = synth.workload_pair("prop128_s3_a10", seed=0)
+        for name, (src, orig) in (("map1", (pair.map1, pair.orig1)), ("map2", (pair.map2, pair.orig2))):
+            m = vg.mrc_obj.from_array(src, 1.0, orig)
+            with contextlib.redirect_stdout(io.StringIO()):
+                _, mn = vg.mrc_set_vox_size(m, 0.1, 3.0)
+            sd = dev.to_dev(m.data)
+            args = (sd, np.float64(m.xwidth), m.orig.astype(np.float64), mn.xdim, 3.0, mn.orig, 16.0)
+            vg.fastvec_device(*args, dev=dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(10):
+                vg.fastvec_device(*args, dev=dev)
+            e1.record()
+            torch.cuda.synchronize()
+            print(f"fastvec {name} {m.data.shape} -> {mn.xdim}^3: {1000 * e0.elapsed_time(e1) / 10:.1f} us per map")
     elif what == "prop":
         net = P.load_weights(dev)[0]
         maker = P.PairMaker(dev)
