@@ -320,6 +320,9 @@ int vesper_prop_adam(float *w, float *m, float *v, const float *g, int n, float 
 /* idx_out int32[k]: indices of the k largest scores (ties to the lower
  * index), in ascending index order. */
 int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void *stream);
+/* The same for nbatch score rows at once: scores float[nbatch][n] ->
+ * idx_out int32[nbatch][k], one block per row. */
+int vesper_topk_subset_batch(const float *scores, int nbatch, int n, int k, int32_t *idx_out, void *stream);
 
 #ifdef __cplusplus
 }

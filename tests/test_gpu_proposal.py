@@ -173,6 +173,33 @@ def test_topk_subset(dev, n, k):
     assert np.array_equal(got, want)
 
 
+def test_topk_subset_batch_rows(dev):
+    """vesper_topk_subset_batch: each row's selection equals the one-row call."""
+    from vesper_python_gb300 import proposal as P
+    rng = np.random.default_rng(3)
+    s = np.round(rng.normal(size=(5, 24624)) * 20) / 4
+    st = dev.to_dev(s, torch.float32)
+    got = P.subset_from_scores(dev, st, 0.05).cpu().numpy()
+    for i in range(5):
+        want = P.subset_from_scores(dev, st[i].contiguous(), 0.05).cpu().numpy()
+        assert np.array_equal(got[i], want)
+
+
+def test_rotation_scores_many_equals_one_pair(dev):
+    """Three pairs encoded and scored together give each pair's scores bit for
+    bit (the encoder's blocks never mix maps)."""
+    net = _net(dev, seed=13)
+    rng = np.random.default_rng(14)
+    d = 9
+    fields = dev.to_dev(np.stack([_field(rng, d) for _ in range(6)]), torch.float32)
+    from vesper_python_gb300 import vesper as vg
+    mats = dev.to_dev(vg.rot_matrices(orc.calc_angle_comb(30.0)[::3]))
+    many = net.rotation_scores_many(fields, mats).cpu().numpy()
+    for i in range(3):
+        one = net.rotation_scores(fields[2 * i:2 * i + 2].contiguous(), mats).cpu().numpy()
+        assert np.array_equal(many[i], one)
+
+
 def test_inference_scores_match_training_scores(dev):
     """rotation_scores (stacked encoder pass, voxel-major float4 scoring)
     against encode + vesper_prop_score on the same fields."""

@@ -143,6 +143,7 @@ SIGNATURES = {
     "vesper_prop_adam": [_vp, _vp, _vp, _vp, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _i,
                          ctypes.c_float, _vp, _vp],
     "vesper_topk_subset": [_vp, _i, _i, _vp, _vp],
+    "vesper_topk_subset_batch": [_vp, _i, _i, _i, _vp, _vp],
 }
 
 

@@ -352,8 +352,7 @@ class Aligner:
             st.launches += 2
         if p.proposal is not None:
             self._mark("proposal")
-            for st in P:
-                self._proposal_subset(p, st, mats)
+            self._proposal_subsets(p, P, mats)
         self._mark("search")
         for st in P:
             self._global_search(p, st, mats if st.order is None else st.sub, nang)
@@ -413,21 +412,29 @@ class Aligner:
         self.d2h_bytes += sum(a.nbytes for g in res for a in g)
         return res
 
-    def _proposal_subset(self, p, st, mats):
+    def _proposal_subsets(self, p, P, mats):
         """Network scores of every rotation and the exact-search subset
-        (ascending grid indices) of one pair; all on the device."""
+        (ascending grid indices) of every pair; all on the device.  Pairs of
+        one pooled side share the encoder launches (one per layer for all
+        their maps) and one top-k launch."""
         from . import proposal as prop
         dev = self.dev
         pool = int(p.proposal_pool)
-        dim = st.dim
-        dp = (dim + pool - 1) // pool
-        fTQ = torch.empty((2, 4, dp, dp, dp), dtype=torch.float32, device=dev.device)
-        prop.map_field(st.tdata, st.tvec, pool, dev, out=fTQ[0])
-        prop.map_field(st.qdata, st.qvec, pool, dev, out=fTQ[1])
-        s = p.proposal.rotation_scores(fTQ, mats)
-        st.order = prop.subset_from_scores(dev, s, p.proposal_frac).to(torch.int64)
-        st.sub = mats.index_select(0, st.order)
-        st.launches += 9
+        groups = {}
+        for st in P:
+            groups.setdefault((st.dim + pool - 1) // pool, []).append(st)
+        for dp, sts in groups.items():
+            fTQ = torch.empty((2 * len(sts), 4, dp, dp, dp), dtype=torch.float32, device=dev.device)
+            for i, st in enumerate(sts):
+                prop.map_field(st.tdata, st.tvec, pool, dev, out=fTQ[2 * i])
+                prop.map_field(st.qdata, st.qvec, pool, dev, out=fTQ[2 * i + 1])
+            s = p.proposal.rotation_scores_many(fTQ, mats)
+            orders = prop.subset_from_scores(dev, s, p.proposal_frac).to(torch.int64)
+            for i, st in enumerate(sts):
+                st.order = orders[i]
+                st.sub = mats.index_select(0, st.order)
+                # 2 fields + (4 layers + vmajor + top-k) shared by the group + scoring
+                st.launches += 3 + (6 if i == 0 else 0)
 
     def _global_search(self, p, st, mats, nang):
         """Search of the given rotations, top-N and (subset searches) the

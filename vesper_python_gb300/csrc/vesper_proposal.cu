@@ -555,6 +555,8 @@ __global__ void __launch_bounds__(1024) k_topk_subset(const float *s, int n, int
     __shared__ int ncount[1024 / 32];
     __shared__ uint32_t sel_digit, sel_need;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    s += (size_t)blockIdx.x * n;     // block b: score row b
+    idx += (size_t)blockIdx.x * k;
     if (skeys) {
         for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = float_order(s[i]);
     }
@@ -848,14 +850,20 @@ extern "C" int vesper_prop_adam(float *w, float *m, float *v, const float *g, in
     return VESPER_OK;
 }
 
-extern "C" int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void *stream) {
-    if (!scores || !idx_out || n < 1 || k < 1 || k > n) return fail(VESPER_ERR_INVALID, "topk_subset: bad args");
+extern "C" int vesper_topk_subset_batch(const float *scores, int nbatch, int n, int k, int32_t *idx_out,
+                                        void *stream) {
+    if (!scores || !idx_out || nbatch < 1 || nbatch > 65535 || n < 1 || k < 1 || k > n)
+        return fail(VESPER_ERR_INVALID, "topk_subset: bad args");
     const size_t hb = (size_t)kTkWarps * 256 * sizeof(uint32_t);
     const size_t kb = (size_t)n * sizeof(uint32_t);
     const int skeys = hb + kb <= (size_t)smem_limit() - 4096 ? 1 : 0;
     const size_t sm = hb + (skeys ? kb : 0);
     allow_smem(k_topk_subset, sm);
-    k_topk_subset<<<1, 1024, sm, (cudaStream_t)stream>>>(scores, n, k, idx_out, skeys);
+    k_topk_subset<<<nbatch, 1024, sm, (cudaStream_t)stream>>>(scores, n, k, idx_out, skeys);
     VG_CHECK_LAUNCH("k_topk_subset");
     return VESPER_OK;
+}
+
+extern "C" int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void *stream) {
+    return vesper_topk_subset_batch(scores, 1, n, k, idx_out, stream);
 }

@@ -162,26 +162,37 @@ class ProposalNet:
         every rotation (one encoder pass over the stack, voxel-major
         features: float16 with vesper_prop_score_f16, else float32 with
         vesper_prop_score_vm)."""
+        return self.rotation_scores_many(fTQ, mats, half)[0]
+
+    def rotation_scores_many(self, fTQ, mats, half=True):
+        """Inference for P pairs of one pooled side at once: fields
+        [2P][4][d][d][d] (target and query of pair i at 2i, 2i + 1) -> scores
+        [P][nrot], with one encoder launch per layer and one voxel-major
+        conversion for all 2P maps, then one scoring launch per pair."""
         d = int(fTQ.shape[-1])
+        nm = int(fTQ.shape[0])
+        npair = nm // 2
         K = CHANNELS[-1]
-        feat = self.encode(fTQ, nmap=2)[-1]
+        feat = self.encode(fTQ, nmap=nm)[-1]
         n = int(mats.shape[0])
-        s = torch.empty(n, dtype=torch.float32, device=self.dev.device)
+        s = torch.empty((npair, n), dtype=torch.float32, device=self.dev.device)
         if half:
-            vm = torch.empty((2, d * d * d, K), dtype=torch.float16, device=self.dev.device)
-            _native.check(self.lib.vesper_prop_vmajor_f16(_p(feat), K, d, 2, _p(vm), self.dev.stream))
+            vm = torch.empty((nm, d * d * d, K), dtype=torch.float16, device=self.dev.device)
+            _native.check(self.lib.vesper_prop_vmajor_f16(_p(feat), K, d, nm, _p(vm), self.dev.stream))
             sm = srcmap(self.dev, d, mats)
-            if sm is not None:
-                _native.check(self.lib.vesper_prop_score_map(_p(vm[0]), _p(vm[1]), K, d, _p(sm), n, _p(s),
-                                                             self.dev.stream))
-            else:
-                _native.check(self.lib.vesper_prop_score_f16(_p(vm[0]), _p(vm[1]), K, d, _p(mats), n, _p(s),
-                                                             self.dev.stream))
+            for i in range(npair):
+                if sm is not None:
+                    _native.check(self.lib.vesper_prop_score_map(_p(vm[2 * i]), _p(vm[2 * i + 1]), K, d, _p(sm), n,
+                                                                 _p(s[i]), self.dev.stream))
+                else:
+                    _native.check(self.lib.vesper_prop_score_f16(_p(vm[2 * i]), _p(vm[2 * i + 1]), K, d, _p(mats), n,
+                                                                 _p(s[i]), self.dev.stream))
         else:
-            vm = torch.empty((2, d * d * d, K), dtype=torch.float32, device=self.dev.device)
-            _native.check(self.lib.vesper_prop_vmajor(_p(feat), K, d, 2, _p(vm), self.dev.stream))
-            _native.check(self.lib.vesper_prop_score_vm(_p(vm[0]), _p(vm[1]), K, d, _p(mats), n, _p(s),
-                                                        self.dev.stream))
+            vm = torch.empty((nm, d * d * d, K), dtype=torch.float32, device=self.dev.device)
+            _native.check(self.lib.vesper_prop_vmajor(_p(feat), K, d, nm, _p(vm), self.dev.stream))
+            for i in range(npair):
+                _native.check(self.lib.vesper_prop_score_vm(_p(vm[2 * i]), _p(vm[2 * i + 1]), K, d, _p(mats), n,
+                                                            _p(s[i]), self.dev.stream))
         return s
 
     def propose(self, fTQ, mats, frac):
@@ -429,10 +440,13 @@ def baseline_scores(dev, pf: PairFields, mats, kind):
 
 
 def subset_from_scores(dev, s, frac):
-    n = int(s.numel())
+    """Grid indices (int32, ascending) of the best ``frac`` of the scores ``s``
+    [n], or, for a score matrix [P][n], of each row ([P][k], one launch)."""
+    rows = 1 if s.dim() == 1 else int(s.shape[0])
+    n = int(s.shape[-1])
     k = max(1, int(math.ceil(frac * n)))
-    idx = torch.empty(k, dtype=torch.int32, device=dev.device)
-    _native.check(dev.lib.vesper_topk_subset(_p(s), n, k, _p(idx), dev.stream))
+    idx = torch.empty((rows, k) if s.dim() > 1 else (k,), dtype=torch.int32, device=dev.device)
+    _native.check(dev.lib.vesper_topk_subset_batch(_p(s.contiguous()), rows, n, k, _p(idx), dev.stream))
     return idx
 
 
