@@ -171,7 +171,16 @@ def check(rc: int):
         raise VesperError(rc, msg)
 
 
+_SIZES: dict = {}
+
+
 def size_query(fn_name, *args) -> int:
-    out = ctypes.c_size_t(0)
-    check(getattr(load(), fn_name)(*args, ctypes.byref(out)))
-    return int(out.value)
+    """A ``*_size``/``*_bytes`` query of the library (a pure function of its
+    integer arguments, so answers are memoised)."""
+    key = (fn_name,) + args
+    v = _SIZES.get(key)
+    if v is None:
+        out = ctypes.c_size_t(0)
+        check(getattr(load(), fn_name)(*args, ctypes.byref(out)))
+        v = _SIZES[key] = int(out.value)
+    return v

@@ -218,17 +218,11 @@ class Aligner:
         if p.A > 5.0:
             self._mark("refine")
         for i, st in enumerate(P):
-            raw, lin_h, toph = glob[i][0], glob[i][1], glob[i][2]
-            top_h = [int(t) for t in toph if t >= 0]
-            raw_grid, lin_grid = raw, lin_h
+            top_h = [int(t) for t in glob[i][2] if t >= 0]
             if st.order is not None:
                 # subset positions -> grid indices (the subset is in ascending grid order)
-                gi = glob[i][3]
-                raw_grid = np.zeros(nang, raw.dtype)
-                lin_grid = np.zeros(nang, lin_h.dtype)
-                raw_grid[gi] = raw
-                lin_grid[gi] = lin_h
-                top_h = [int(gi[t]) for t in top_h]
+                top_h = [int(glob[i][3][t]) for t in top_h]
+            st.top_h = top_h
             rd3 = 1.0 / st.dim ** 3
             scale = 1.0
             if mode == "CC":
@@ -237,29 +231,50 @@ class Aligner:
                 scale = 1.0 / sh[i, 4] ** 2
             rd3s.append(rd3)
             scales.append(scale)
-            # statistics over the correlated rotations (the whole grid, or the subset)
-            score_arr = raw.astype(np.float64) * scale * rd3
-            st.ave_s, st.std_s = float(np.mean(score_arr)), float(np.std(score_arr))
-            score_grid = raw_grid.astype(np.float64) * scale * rd3
-            st.top_list = [(tuple(angle_comb[r]), float(score_grid[r]), vg.unravel(lin_grid[r], st.dim))
-                           for r in top_h]
-            st.top_h = top_h
+
+        def global_lists():
+            # statistics over the correlated rotations (the whole grid, or the
+            # subset) and the global top-N list; run while the refinement
+            # searches are on the device
+            for i, st in enumerate(P):
+                raw, lin_h = glob[i][0], glob[i][1]
+                raw_grid, lin_grid = raw, lin_h
+                if st.order is not None:
+                    gi = glob[i][3]
+                    raw_grid = np.zeros(nang, raw.dtype)
+                    lin_grid = np.zeros(nang, lin_h.dtype)
+                    raw_grid[gi] = raw
+                    lin_grid[gi] = lin_h
+                score_arr = raw.astype(np.float64) * scales[i] * rd3s[i]
+                st.ave_s, st.std_s = float(np.mean(score_arr)), float(np.std(score_arr))
+                score_grid = raw_grid.astype(np.float64) * scales[i] * rd3s[i]
+                st.top_list = [(tuple(angle_comb[r]), float(score_grid[r]), vg.unravel(lin_grid[r], st.dim))
+                               for r in st.top_h]
+
         # ---- 4. refinement around each pair's top-N: every pair's angle set and
         # matrices at once (one index copy and one gather from the lattice
-        # table), then the searches
+        # table), then the searches.  The +-5 degree sets of neighbouring top-N
+        # angles overlap and the reference keeps the duplicates (:689-713); a
+        # rotation's result depends on its angle alone, so each distinct angle
+        # is searched once and the results are expanded back to the full list
+        # (same scores, same order, same stable top-N).
         if p.A > 5.0:
             sets = [vg.refine_angle_list([angle_comb[r] for r in st.top_h]) for st in P]
-            allm = vg.rot_matrices_lattice(np.concatenate(sets), dev)
-            off = 0
-            for st, ra in zip(P, sets):
+            allm, counts, inv_all = self._distinct_rotations(sets)
+            off = ioff = 0
+            for st, ra, nu in zip(P, sets, counts):
                 st.ref_angles = ra
-                rmats = allm[off:off + len(ra)]
-                off += len(ra)
-                st.rs, st.rl = vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats, batch=p.batch,
-                                                dev=dev, tuned=True)
-                st.launches += self._search_launches(st.dim, mode, len(st.ref_angles), p.batch)
+                rmats = allm[off:off + nu]
+                sel = inv_all[ioff:ioff + len(ra)]
+                off += nu
+                ioff += len(ra)
+                rs, rl = vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats, batch=p.batch, dev=dev,
+                                          tuned=True)
+                st.launches += self._search_launches(st.dim, mode, nu, p.batch)
+                st.rs, st.rl = rs.index_select(0, sel), rl.index_select(0, sel)
                 st.rtop = vg.topn_device(st.rs, p.N, dev=dev)
                 st.launches += 1
+        global_lists()
         # ---- 5. rotated top-N models and their float64 scores -------------------
         if p.A > 5.0:
             ref = self._fetch([[st.rs[:, 0].contiguous(), st.rl[:, 0].contiguous(), st.rtop] for st in P])
@@ -321,6 +336,29 @@ class Aligner:
         self._close_marks()
         return out
 
+    def _distinct_rotations(self, sets):
+        """Matrices of the distinct angles of every pair's angle list (pair by
+        pair, consecutive), their count per pair, and for every entry of the
+        concatenated lists its row within its pair's block (device int64):
+        entry j of pair i is row inv[j] of that pair's distinct matrices."""
+        dev = self.dev
+        lens = np.array([len(ra) for ra in sets], np.int64)
+        allang = np.concatenate(sets) if len(sets) else np.zeros((0, 3))
+        key = vg.lattice_index(allang)
+        if key is None:     # off the 5-degree lattice: per pair, on the angles
+            uniq = [np.unique(ra, axis=0, return_inverse=True) for ra in sets]
+            allm = vg.rot_matrices_lattice(np.concatenate([u for u, _ in uniq]), dev)
+            inv = np.concatenate([iv.reshape(-1) for _, iv in uniq]).astype(np.int64)
+            return allm, [len(u) for u, _ in uniq], dev.to_dev_async(inv)
+        span = vg.LATTICE_N ** 3
+        pid = np.repeat(np.arange(len(sets), dtype=np.int64), lens)
+        ukeys, inv = np.unique(pid * span + key, return_inverse=True)
+        upid = ukeys // span
+        counts = np.bincount(upid, minlength=len(sets))
+        starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+        allm = vg.lattice_rot_matrices_device(dev).index_select(0, dev.to_dev_async(ukeys % span))
+        return allm, [int(c) for c in counts], dev.to_dev_async(inv.reshape(-1) - starts[pid])
+
     def _global_stage(self, P, p, mats, nang):
         """fastVEC of both maps, target statistics and spectra, proposal subset
         and global search of every pair (device work only, except the
@@ -333,9 +371,11 @@ class Aligner:
         for i, st in enumerate(P):
             dim = st.dim
             st.tdata, _, st.tvec = vg.fastvec_device(st.src1, np.float64(np.float32(st.width1)),
-                                                     st.o1.astype(np.float64), dim, p.s, st.no1, p.g, dev=dev)
+                                                     st.o1.astype(np.float64), dim, p.s, st.no1, p.g, dev=dev,
+                                                     want_f32=False)
             st.qdata, _, st.qvec = vg.fastvec_device(st.src2, np.float64(np.float32(st.width2)),
-                                                     st.o2.astype(np.float64), dim, p.s, st.no2, p.g, dev=dev)
+                                                     st.o2.astype(np.float64), dim, p.s, st.no2, p.g, dev=dev,
+                                                     want_f32=False)
             ws = dev.workspace(("stats", dim), _native.size_query("vesper_map_stats_workspace_size", dim))
             _native.check(self.lib.vesper_map_stats_ws(ctypes.c_void_p(st.tdata.data_ptr()), dim,
                                                        ctypes.c_void_p(stats[i].data_ptr()),

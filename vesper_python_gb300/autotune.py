@@ -32,8 +32,13 @@ def _cache_path():
     return p or None
 
 
+_NAMES: dict = {}
+
+
 def _key(dim, mode, dev):
-    name = torch.cuda.get_device_name(dev.device) if torch.cuda.is_available() else "cpu"
+    name = _NAMES.get(dev.device)
+    if name is None:
+        name = _NAMES[dev.device] = torch.cuda.get_device_name(dev.device) if torch.cuda.is_available() else "cpu"
     return f"{name}|d={dim}|mode={mode}"
 
 

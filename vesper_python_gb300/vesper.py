@@ -46,6 +46,14 @@ MODE_CODES = {"VecProduct": 0, "Overlap": 1, "CC": 2, "PCC": 3, "Laplacian": 4, 
 # device plumbing
 # ----------------------------------------------------------------------------
 
+def _raw_stream(index):
+    return torch.cuda.current_stream(index).cuda_stream
+
+
+if hasattr(torch._C, "_cuda_getCurrentRawStream"):
+    _raw_stream = torch._C._cuda_getCurrentRawStream   # noqa: F811  (same value, without the Stream object)
+
+
 class Device:
     """CUDA device, stream and cached scratch buffers for the C-ABI calls."""
 
@@ -53,12 +61,15 @@ class Device:
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 VESPER path needs a CUDA device; none is available")
         self.device = torch.device(device)
+        self.index = self.device.index if self.device.index is not None else torch.cuda.current_device()
         self.lib = _native.load()
         self._ws = {}
 
     @property
     def stream(self):
-        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        """The current CUDA stream of this device (a capture stream inside
+        torch.cuda.graph), as the raw handle the C-ABI takes."""
+        return ctypes.c_void_p(_raw_stream(self.index))
 
     def workspace(self, key, nbytes):
         buf = self._ws.get(key)
@@ -207,17 +218,19 @@ def mrc_set_vox_size(mrc, th=0.00, voxel_size=7.0):
 # fastVEC
 # ----------------------------------------------------------------------------
 
-def fastvec_device(src_data, src_width, src_orig, dim, dest_width, dest_orig, dreso, dev=None):
+def fastvec_device(src_data, src_width, src_orig, dim, dest_width, dest_orig, dreso, dev=None, want_f32=True):
     """vesper_fastvec on device arrays.  ``src_data`` is a host [x][y][z] array or
-    a float32 CUDA tensor.  Returns (data f64, data f32, vec f32) CUDA tensors."""
+    a float32 CUDA tensor.  Returns (data f64, data f32 or None when not
+    ``want_f32``, vec f32) CUDA tensors."""
     dev = dev or default_device()
     src = src_data if isinstance(src_data, torch.Tensor) else dev.to_dev(np.asarray(src_data, np.float32))
-    src = src.to(torch.float32).contiguous()
+    if src.dtype != torch.float32 or not src.is_contiguous():
+        src = src.to(torch.float32).contiguous()
     sx, sy, sz = src.shape
     ws_bytes = _native.size_query("vesper_fastvec_workspace_size", sx, sy, sz, dim)
     ws = dev.workspace(("fastvec", sx, sy, sz, dim), ws_bytes)
     data = torch.empty((dim, dim, dim), dtype=torch.float64, device=dev.device)
-    data32 = torch.empty((dim, dim, dim), dtype=torch.float32, device=dev.device)
+    data32 = torch.empty((dim, dim, dim), dtype=torch.float32, device=dev.device) if want_f32 else None
     vec = torch.empty((dim, dim, dim, 3), dtype=torch.float32, device=dev.device)
     _native.check(dev.lib.vesper_fastvec(_ptr(src), sx, sy, sz, float(src_width), _host_d3(src_orig), int(dim),
                                          float(dest_width), _host_d3(dest_orig), float(dreso), _ptr(data),
@@ -421,7 +434,8 @@ def target_spectra_device(data, vec, mode, ave, probs=None, dev=None):
 
 
 _TUNED = {}          # (device, side, mode) -> the autotuner's launch shape
-_SEARCH_SIZES = {}   # (side, mode, mixed, batch, rotations) -> (scores per rotation, workspace bytes)
+_SEARCH_SIZES = {}   # (device, side, mode, mixed, batch, rotations, options) -> (scores per rotation,
+#                      workspace tensor, options array)
 
 
 def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, batch=0, dev=None, profile=None,
@@ -442,19 +456,20 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
             _TUNED[tk] = t
         batch = int(t["batch"])
         opts = (-1, int(t["cchunk"]), int(t["W"]))
-    sk = (d, code, mix is not None, int(batch), max(n, 1))
-    sz = _SEARCH_SIZES.get(sk)
-    if sz is None:
-        sz = _SEARCH_SIZES[sk] = (dev.lib.vesper_search_nscore(code, 1 if mix is not None else 0),
-                                  _native.size_query("vesper_search_workspace_size", d, code, int(batch), max(n, 1)))
-    nscore, ws_bytes = sz
+    # per call shape: scores per rotation, the workspace and the options array
+    sk = (dev.device, d, code, mix is not None, int(batch), max(n, 1), tuple(opts) if opts is not None else None)
+    ent = _SEARCH_SIZES.get(sk)
+    if ent is None:
+        ws_bytes = _native.size_query("vesper_search_workspace_size", d, code, int(batch), max(n, 1))
+        ent = _SEARCH_SIZES[sk] = (dev.lib.vesper_search_nscore(code, 1 if mix is not None else 0),
+                                   dev.workspace(("search", d, code, int(batch)), ws_bytes),
+                                   (ctypes.c_int * 3)(*[int(v) for v in opts]) if opts is not None else None)
+    nscore, ws, copts = ent
     scores = torch.empty((n, nscore), dtype=torch.float32, device=dev.device)
     lin = torch.empty((n, nscore), dtype=torch.int32, device=dev.device)
-    ws = dev.workspace(("search", d, code, int(batch)), ws_bytes)
     mixarr = (ctypes.c_double * 5)(*[float(v) for v in mix]) if mix is not None else None
     args = (_ptr(spec), _ptr(data), _ptr(vec), _ptr(probs), d, code, float(ave or 0.0), _ptr(rotmats), n, mixarr,
             _ptr(scores), _ptr(lin), int(batch), _ptr(ws), ws.numel(), dev.stream)
-    copts = (ctypes.c_int * 3)(*[int(v) for v in opts]) if opts is not None else None
     if profile is not None:
         ms = (ctypes.c_float * 4)()
         nl = (ctypes.c_int * 4)()
@@ -691,9 +706,15 @@ def search_map_fft(mrc_target, mrc_search, TopN=10, ang=30, mode="VecProduct", i
     print()
     if ang > 5.0:
         refine_ang_arr = refine_angle_list([s["angle"] for s in sorted_topN])
-        rmats = dev.to_dev(rot_matrices(refine_ang_arr))
+        # the overlapping +-5 degree sets repeat angles (kept, as in the
+        # reference); each distinct angle is searched once and its result
+        # copied to every position it holds
+        uang, uinv = np.unique(refine_ang_arr, axis=0, return_inverse=True)
+        rmats = dev.to_dev(rot_matrices(uang))
         rscores, rlin = search_device(spec, qdata, qvec, mode, mrc_target.ave, rmats, batch=batch, dev=dev,
                                       tuned=True)
+        sel_u = dev.to_dev(uinv.reshape(-1).astype(np.int64))
+        rscores, rlin = rscores.index_select(0, sel_u), rlin.index_select(0, sel_u)
         rtop = [int(i) for i in topn_device(rscores, TopN, dev=dev).cpu().numpy() if i >= 0]
         rraw = rscores[:, 0].cpu().numpy()
         rlin_h = rlin[:, 0].cpu().numpy()
@@ -779,8 +800,13 @@ def search_map_fft_prob(mrc_P1, mrc_P2, mrc_P3, mrc_P4, mrc_target, mrc_search, 
     if ang > 5.0:
         print("\n###Start Refining###")
         refine_ang_list = refine_angle_list([s["angle"] for s in sorted_topN])
-        rmats = dev.to_dev(rot_matrices(refine_ang_list))
+        # each distinct angle searched once (the mixed score of a rotation
+        # depends on it alone once the statistics are fixed), then expanded
+        uang, uinv = np.unique(refine_ang_list, axis=0, return_inverse=True)
+        rmats = dev.to_dev(rot_matrices(uang))
         rs, rl = search_device(spec, qdata, qvec, "prob", 0.0, rmats, probs=qprobs, mix=mix, batch=batch, dev=dev)
+        sel_u = dev.to_dev(uinv.reshape(-1).astype(np.int64))
+        rs, rl = rs.index_select(0, sel_u), rl.index_select(0, sel_u)
         rtop = [int(i) for i in topn_device(rs, TopN, column=2, dev=dev).cpu().numpy() if i >= 0]
         rsh = rs.cpu().numpy()
         rlh = rl.cpu().numpy()
