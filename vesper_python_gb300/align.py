@@ -359,6 +359,13 @@ class Aligner:
         allm = vg.lattice_rot_matrices_device(dev).index_select(0, dev.to_dev_async(ukeys % span))
         return allm, [int(c) for c in counts], dev.to_dev_async(inv.reshape(-1) - starts[pid])
 
+    FV_STREAMS = 4
+
+    def _side_streams(self):
+        if getattr(self, "_side", None) is None:
+            self._side = [torch.cuda.Stream(self.dev.device) for _ in range(self.FV_STREAMS)]
+        return self._side
+
     def _global_stage(self, P, p, mats, nang):
         """fastVEC of both maps, target statistics and spectra, proposal subset
         and global search of every pair (device work only, except the
@@ -368,28 +375,48 @@ class Aligner:
         n = len(P)
         self._mark("fastvec")
         stats = torch.empty((n, 5), dtype=torch.float64, device=dev.device)
+        # fastVEC and statistics of the pairs on FV_STREAMS side streams: one
+        # map's kernels fill only part of the GPU (latency-bound, 10^2-10^3
+        # blocks), so pairs overlap; the streams fork from and join the current
+        # stream (also inside a CUDA-graph capture)
+        cur = torch.cuda.current_stream(dev.device)
+        capturing = torch.cuda.is_current_stream_capturing()   # the graph's pool keeps its blocks
+        side = self._side_streams()
+        for sd in side:
+            sd.wait_stream(cur)
         for i, st in enumerate(P):
             dim = st.dim
-            st.tdata, _, st.tvec = vg.fastvec_device(st.src1, np.float64(np.float32(st.width1)),
-                                                     st.o1.astype(np.float64), dim, p.s, st.no1, p.g, dev=dev,
-                                                     want_f32=False)
-            st.qdata, _, st.qvec = vg.fastvec_device(st.src2, np.float64(np.float32(st.width2)),
-                                                     st.o2.astype(np.float64), dim, p.s, st.no2, p.g, dev=dev,
-                                                     want_f32=False)
-            ws = dev.workspace(("stats", dim), _native.size_query("vesper_map_stats_workspace_size", dim))
-            _native.check(self.lib.vesper_map_stats_ws(ctypes.c_void_p(st.tdata.data_ptr()), dim,
-                                                       ctypes.c_void_p(stats[i].data_ptr()),
-                                                       ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
+            with torch.cuda.stream(side[i % len(side)]):
+                st.tdata, _, st.tvec = vg.fastvec_device(st.src1, np.float64(np.float32(st.width1)),
+                                                         st.o1.astype(np.float64), dim, p.s, st.no1, p.g, dev=dev,
+                                                         want_f32=False)
+                st.qdata, _, st.qvec = vg.fastvec_device(st.src2, np.float64(np.float32(st.width2)),
+                                                         st.o2.astype(np.float64), dim, p.s, st.no2, p.g, dev=dev,
+                                                         want_f32=False)
+                ws = dev.workspace(("stats", dim), _native.size_query("vesper_map_stats_workspace_size", dim))
+                _native.check(self.lib.vesper_map_stats_ws(ctypes.c_void_p(st.tdata.data_ptr()), dim,
+                                                           ctypes.c_void_p(stats[i].data_ptr()),
+                                                           ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
+                if mode not in ("PCC", "CC"):     # spectra need no host value: same stream
+                    st.ave = 0.0
+                    st.spec = vg.target_spectra_device(st.tdata, st.tvec, mode, st.ave, dev=dev)
+                    st.launches += 2
+            if not capturing:
+                for t in (st.tdata, st.tvec, st.qdata, st.qvec) + ((st.spec,) if mode not in ("PCC", "CC") else ()):
+                    t.record_stream(cur)    # made on a side stream, used on this one
             st.launches += 12
+        for sd in side:
+            cur.wait_stream(sd)
         sh = None
         if mode in ("PCC", "CC"):
             sh = stats.cpu().numpy()
             self.d2h_bytes += sh.nbytes
         self._mark("spectra")
-        for i, st in enumerate(P):
-            st.ave = float(sh[i, 2]) if sh is not None else 0.0
-            st.spec = vg.target_spectra_device(st.tdata, st.tvec, mode, st.ave, dev=dev)
-            st.launches += 2
+        if sh is not None:      # CC / PCC: the spectra use the target's mean
+            for i, st in enumerate(P):
+                st.ave = float(sh[i, 2])
+                st.spec = vg.target_spectra_device(st.tdata, st.tvec, mode, st.ave, dev=dev)
+                st.launches += 2
         if p.proposal is not None:
             self._mark("proposal")
             self._proposal_subsets(p, P, mats)

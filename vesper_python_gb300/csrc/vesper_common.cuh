@@ -6,6 +6,9 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "vesper_fft.cuh"
 #include "../../include/vesper_gb300.h"
@@ -189,9 +192,28 @@ inline int smem_limit() {
     return lim;
 }
 
+// Raise a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device.  The largest limit set so far is remembered per (device,
+// kernel), so the driver call is made only when a launch needs more (the call
+// costs about a microsecond of host time, and hot paths launch thousands of
+// kernels).
 template <typename K>
 inline void allow_smem(K kernel, size_t bytes) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> set;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const std::pair<int, const void *> key(dev, (const void *)kernel);
+    {
+        std::lock_guard<std::mutex> g(mu);
+        const auto it = set.find(key);
+        if (it != set.end() && it->second >= bytes) return;
+    }
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) {
+        std::lock_guard<std::mutex> g(mu);
+        size_t &v = set[key];
+        if (bytes > v) v = bytes;
+    }
 }
 
 }  // namespace vg

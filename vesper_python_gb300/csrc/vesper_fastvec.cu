@@ -751,10 +751,10 @@ extern "C" int vesper_fastvec(const float *src, int sx, int sy, int sz, double s
         VG_CHECK_LAUNCH("k_fvf_rows");
         const unsigned zb = (unsigned)((nrows + kZRows - 1) / kZRows);
         if (zsw) {
-            cudaFuncSetAttribute(k_fvf_z<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
+            allow_smem(k_fvf_z<true>, s1);
             k_fvf_z<true><<<zb, 256, s1, st>>>(src, g, t, a0, a1);
         } else {
-            cudaFuncSetAttribute(k_fvf_z<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
+            allow_smem(k_fvf_z<false>, s1);
             k_fvf_z<false><<<zb, 256, s1, st>>>(src, g, t, a0, a1);
         }
         VG_CHECK_LAUNCH("k_fvf_z");
@@ -763,10 +763,10 @@ extern "C" int vesper_fastvec(const float *src, int sx, int sy, int sz, double s
         size_t sy2, sx3;
         fvf_chunk(g, sy, 2, &yc, &ry, &sy2);
         fvf_chunk(g, sx, 3, &xc, &rx, &sx3);
-        cudaFuncSetAttribute(k_fvf_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy2);
+        allow_smem(k_fvf_y, sy2);
         k_fvf_y<<<dim3(zt, sx, (unsigned)((dim + yc - 1) / yc)), 256, sy2, st>>>(g, t, yc, ry, a0, a1, b0, b1, b2);
         VG_CHECK_LAUNCH("k_fvf_y");
-        cudaFuncSetAttribute(k_fvf_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx3);
+        allow_smem(k_fvf_x, sx3);
         k_fvf_x<<<dim3(zt, dim, (unsigned)((dim + xc - 1) / xc)), 256, sx3, st>>>(src, g, t, xc, rx, b0, b1, b2,
                                                                                   data_out, data_f32, vec_out);
         VG_CHECK_LAUNCH("k_fvf_x");
@@ -774,17 +774,17 @@ extern "C" int vesper_fastvec(const float *src, int sx, int sy, int sz, double s
     }
     const size_t s1 = (size_t)kRB * sz * sizeof(float);
     if (s1 > 200 * 1024) return fail(VESPER_ERR_UNSUPPORTED, "vesper_fastvec: source rows too long (%d)", sz);
-    cudaFuncSetAttribute(k_fv_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
+    allow_smem(k_fv_z, s1);
     k_fv_z<<<(unsigned)((nrows + kRB - 1) / kRB), 256, s1, st>>>(src, g, t, A0, A1);
     VG_CHECK_LAUNCH("k_fv_z");
     const size_t s2 = 2 * (size_t)sy * kZT * sizeof(double);
     const size_t s3 = 3 * (size_t)sx * kZT3 * sizeof(double);
     if (s2 > 220 * 1024 || s3 > 220 * 1024)
         return fail(VESPER_ERR_UNSUPPORTED, "vesper_fastvec: source side too large (%d, %d)", sx, sy);
-    cudaFuncSetAttribute(k_fv_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2);
+    allow_smem(k_fv_y, s2);
     k_fv_y<<<dim3((dim + kZT - 1) / kZT, sx), 256, s2, st>>>(g, t, A0, A1, B0, B1, B2);
     VG_CHECK_LAUNCH("k_fv_y");
-    cudaFuncSetAttribute(k_fv_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s3);
+    allow_smem(k_fv_x, s3);
     k_fv_x<<<dim3((dim + kZT3 - 1) / kZT3, dim), 256, s3, st>>>(src, g, t, B0, B1, B2, data_out, data_f32, vec_out);
     VG_CHECK_LAUNCH("k_fv_x");
     return VESPER_OK;

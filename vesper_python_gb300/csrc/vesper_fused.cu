@@ -205,12 +205,26 @@ static int launch_fused(const FusedArgs &a, cudaStream_t st) {
     constexpr size_t sm = fused_smem<NCH, D>();
     if (sm > (size_t)smem_limit()) return fail(VESPER_ERR_UNSUPPORTED, "fused search: side %d too large", D);
     allow_smem(k_fused<MODE, NCH, D>, sm);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused<MODE, NCH, D>, kFusedThreads, sm);
-    int dev = 0, nsm = 0;
+    // resident CTAs of the whole GPU, queried once per device
+    static std::mutex mu;
+    static std::map<int, int> slots;
+    int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = std::max(1, std::min(a.nrot, std::max(per_sm, 1) * std::max(nsm, 1)));
+    int cap = 0;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        const auto it = slots.find(dev);
+        if (it != slots.end()) cap = it->second;
+    }
+    if (cap == 0) {
+        int per_sm = 0, nsm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused<MODE, NCH, D>, kFusedThreads, sm);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cap = std::max(per_sm, 1) * std::max(nsm, 1);
+        std::lock_guard<std::mutex> g(mu);
+        slots[dev] = cap;
+    }
+    const int grid = std::max(1, std::min(a.nrot, cap));
     k_fused<MODE, NCH, D><<<grid, kFusedThreads, sm, st>>>(a);
     VG_CHECK_LAUNCH("k_fused");
     return VESPER_OK;

@@ -72,6 +72,9 @@ class Device:
         return ctypes.c_void_p(_raw_stream(self.index))
 
     def workspace(self, key, nbytes):
+        """Scratch buffer for ``key`` on the current stream (work on different
+        streams never shares scratch)."""
+        key = key + (_raw_stream(self.index),)
         buf = self._ws.get(key)
         if buf is None or buf.numel() < nbytes:
             buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=self.device)
