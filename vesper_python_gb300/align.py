@@ -77,6 +77,11 @@ class AlignResult:
     launches: int = 0
 
 
+_NP_DTYPES = {torch.float32: np.dtype(np.float32), torch.float64: np.dtype(np.float64),
+              torch.int32: np.dtype(np.int32), torch.int64: np.dtype(np.int64), torch.int16: np.dtype(np.int16),
+              torch.uint8: np.dtype(np.uint8)}
+
+
 def _size_grid(dmax2_bits, count, cent, width, orig, s):
     """mrc_set_vox_size (VESPER_1_prob_new.py:81-100) from the device radius."""
     if count == 0:
@@ -421,8 +426,22 @@ class Aligner:
             self._mark("proposal")
             self._proposal_subsets(p, P, mats)
         self._mark("search")
-        for st in P:
-            self._global_search(p, st, mats if st.order is None else st.sub, nang)
+        if p.proposal is not None and P and all(st.order is not None for st in P):
+            # equal subsets: results of all pairs in one buffer, the z-scores of
+            # the subsets' best scores in one reduction
+            k = int(P[0].order.shape[0])
+            nscore = dev.lib.vesper_search_nscore(vg.MODE_CODES[mode], 0)
+            S = torch.empty((n, k, nscore), dtype=torch.float32, device=dev.device)
+            L = torch.empty((n, k, nscore), dtype=torch.int32, device=dev.device)
+            for i, st in enumerate(P):
+                self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
+            sc0 = S[:, :, 0]
+            z = (sc0.max(dim=1).values - sc0.mean(dim=1)) / (sc0.std(dim=1) + 1e-30)
+            for i, st in enumerate(P):
+                st.z = z[i]
+        else:
+            for st in P:
+                self._global_search(p, st, mats if st.order is None else st.sub, nang)
         return stats, sh
 
     _STAGE_FIELDS = ("tdata", "tvec", "qdata", "qvec", "ave", "spec", "order", "sub", "scores", "lin", "top", "z",
@@ -471,12 +490,37 @@ class Aligner:
         return stats
 
     def _fetch(self, groups):
-        """Device tensors (a list of lists) to numpy with one wait: the copies
-        are queued without blocking and the stream is synchronised once."""
-        outs = [[t.to("cpu", non_blocking=True) for t in g] for g in groups]
+        """Device tensors (a list of lists) to numpy with one copy and one
+        wait: the tensors' bytes are packed on the device (8-byte aligned
+        pieces), copied to pinned memory in one transfer, and split on the
+        host."""
+        flat = [t.contiguous().reshape(-1) for g in groups for t in g]
+        if not flat:
+            return [[] for _ in groups]
+        pieces, offs, off = [], [], 0
+        for t in flat:
+            b = t.view(torch.uint8)
+            pad = (-b.numel()) % 8
+            pieces.append(b)
+            if pad:
+                pieces.append(torch.empty(pad, dtype=torch.uint8, device=b.device))   # filler, never read
+            offs.append(off)
+            off += b.numel() + pad
+        packed = torch.cat(pieces)
+        host = torch.empty(packed.numel(), dtype=torch.uint8, pin_memory=True)
+        host.copy_(packed, non_blocking=True)
         torch.cuda.current_stream(self.dev.device).synchronize()
-        res = [[o.numpy() for o in g] for g in outs]
-        self.d2h_bytes += sum(a.nbytes for g in res for a in g)
+        buf = host.numpy()
+        it = iter(zip(flat, offs))
+        res = []
+        for g in groups:
+            row = []
+            for t in g:
+                ft, o = next(it)
+                dt = _NP_DTYPES[ft.dtype]
+                row.append(buf[o:o + ft.numel() * dt.itemsize].view(dt).reshape(tuple(t.shape)))
+            res.append(row)
+        self.d2h_bytes += packed.numel()
         return res
 
     def _proposal_subsets(self, p, P, mats):
@@ -497,20 +541,24 @@ class Aligner:
                 prop.map_field(st.qdata, st.qvec, pool, dev, out=fTQ[2 * i + 1])
             s = p.proposal.rotation_scores_many(fTQ, mats)
             orders = prop.subset_from_scores(dev, s, p.proposal_frac).to(torch.int64)
+            subs = mats.index_select(0, orders.reshape(-1)).reshape((len(sts), orders.shape[1]) + tuple(mats.shape[1:]))
             for i, st in enumerate(sts):
                 st.order = orders[i]
-                st.sub = mats.index_select(0, st.order)
+                st.sub = subs[i]
                 # 2 fields + (4 layers + vmajor + top-k) shared by the group + scoring
                 st.launches += 3 + (6 if i == 0 else 0)
 
-    def _global_search(self, p, st, mats, nang):
-        """Search of the given rotations, top-N and (subset searches) the
-        z-score of the best exact score over the subset; all on the device."""
+    def _global_search(self, p, st, mats, nang, out=None, zscore=True):
+        """Search of the given rotations, top-N and (subset searches, unless
+        the caller batches it) the z-score of the best exact score over the
+        subset; all on the device."""
         st.scores, st.lin = vg.search_device(st.spec, st.qdata, st.qvec, p.mode, st.ave, mats, batch=p.batch,
-                                             dev=self.dev, profile=self.profile, tuned=True)
+                                             dev=self.dev, profile=self.profile, tuned=True, out=out)
         st.launches += self._search_launches(st.dim, p.mode, int(mats.shape[0]), p.batch)
         st.top = vg.topn_device(st.scores, p.N, dev=self.dev)
         st.launches += 1
+        if not zscore:
+            return
         if st.order is not None:
             sc0 = st.scores[:, 0]
             st.z = (sc0.max() - sc0.mean()) / (sc0.std() + 1e-30)

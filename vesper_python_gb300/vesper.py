@@ -442,8 +442,9 @@ _SEARCH_SIZES = {}   # (device, side, mode, mixed, batch, rotations, options) ->
 
 
 def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, batch=0, dev=None, profile=None,
-                  opts=None, tuned=False):
-    """vesper_search: (scores f32 [n][nscore], lin int32 [n][nscore]) CUDA tensors.
+                  opts=None, tuned=False, out=None):
+    """vesper_search: (scores f32 [n][nscore], lin int32 [n][nscore]) CUDA tensors,
+    written into ``out`` = (scores, lin) when given (contiguous, those shapes).
     With ``profile`` (a dict), vesper_search_profile runs instead and the dict
     receives the per-pass device milliseconds and launch counts."""
     dev = dev or default_device()
@@ -468,8 +469,14 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
                                    dev.workspace(("search", d, code, int(batch)), ws_bytes),
                                    (ctypes.c_int * 3)(*[int(v) for v in opts]) if opts is not None else None)
     nscore, ws, copts = ent
-    scores = torch.empty((n, nscore), dtype=torch.float32, device=dev.device)
-    lin = torch.empty((n, nscore), dtype=torch.int32, device=dev.device)
+    if out is not None:
+        scores, lin = out
+        if (tuple(scores.shape) != (n, nscore) or tuple(lin.shape) != (n, nscore) or not scores.is_contiguous()
+                or not lin.is_contiguous()):
+            raise ValueError("search_device: out tensors must be contiguous [n][nscore]")
+    else:
+        scores = torch.empty((n, nscore), dtype=torch.float32, device=dev.device)
+        lin = torch.empty((n, nscore), dtype=torch.int32, device=dev.device)
     mixarr = (ctypes.c_double * 5)(*[float(v) for v in mix]) if mix is not None else None
     args = (_ptr(spec), _ptr(data), _ptr(vec), _ptr(probs), d, code, float(ave or 0.0), _ptr(rotmats), n, mixarr,
             _ptr(scores), _ptr(lin), int(batch), _ptr(ws), ws.numel(), dev.stream)
