@@ -89,14 +89,22 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Start sampling every 50 ms; returns once nvidia-smi is answering
+        (its first line, at most 5 s), with that line discarded, so the
+        samples kept are those taken after this call."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except (OSError, ValueError):
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.lines.clear()
 
     def _read(self):
         for line in self.proc.stdout:

@@ -507,8 +507,10 @@ class Aligner:
             offs.append(off)
             off += b.numel() + pad
         packed = torch.cat(pieces)
-        host = torch.empty(packed.numel(), dtype=torch.uint8, pin_memory=True)
-        host.copy_(packed, non_blocking=True)
+        host = getattr(self, "_pinned", None)
+        if host is None or host.numel() < packed.numel():   # one pinned buffer, grown on demand
+            host = self._pinned = torch.empty(max(packed.numel(), 1 << 20), dtype=torch.uint8, pin_memory=True)
+        host[:packed.numel()].copy_(packed, non_blocking=True)
         torch.cuda.current_stream(self.dev.device).synchronize()
         buf = host.numpy()
         it = iter(zip(flat, offs))
@@ -518,7 +520,7 @@ class Aligner:
             for t in g:
                 ft, o = next(it)
                 dt = _NP_DTYPES[ft.dtype]
-                row.append(buf[o:o + ft.numel() * dt.itemsize].view(dt).reshape(tuple(t.shape)))
+                row.append(buf[o:o + ft.numel() * dt.itemsize].view(dt).reshape(tuple(t.shape)).copy())
             res.append(row)
         self.d2h_bytes += packed.numel()
         return res
