@@ -324,6 +324,22 @@ int vesper_topk_subset(const float *scores, int n, int k, int32_t *idx_out, void
  * idx_out int32[nbatch][k], one block per row. */
 int vesper_topk_subset_batch(const float *scores, int nbatch, int n, int k, int32_t *idx_out, void *stream);
 
+/* ---- split-BF16 tensor-core DFT (search pass B) -------------------------- */
+/* Pass B of the search on the 5th-generation tensor cores, on caller-provided
+ * spectra (device pointers, complex64):
+ *   S [nbatch][nch][d][d][d/2+1]  x-untransformed spectra of the rotated query,
+ *   T [nch][d][d][d/2+1]          conjugated target spectra,
+ *   U [nbatch][ngrp][d][d][d/2+1] out: per score group g (channels [0, split)
+ *                                 and [split, nch)) the inverse x DFT of
+ *                                 sum_c T_c * DFT_x(S_c), unnormalised.
+ * The x-axis DFTs run as split-BF16 contractions (hi*hi + hi*lo + lo*hi,
+ * float32 accumulation).  d = 32 or 64.  *err (device int) is set to 1 if a
+ * tensor-core wait timed out.  Replaces the float32 FFT pass B of the search
+ * (fft_search_best_dot, VESPER_1_prob_new.py:464-491, and the prob-mode passes
+ * :880-962) when the search option selects it. */
+int vesper_tc_pass_b(const void *S, const void *T, void *U, int d, int nch, int ngrp, int split, int nbatch, int *err,
+                     void *stream);
+
 #ifdef __cplusplus
 }
 #endif

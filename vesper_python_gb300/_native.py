@@ -144,6 +144,7 @@ SIGNATURES = {
                          ctypes.c_float, _vp, _vp],
     "vesper_topk_subset": [_vp, _i, _i, _vp, _vp],
     "vesper_topk_subset_batch": [_vp, _i, _i, _i, _vp, _vp],
+    "vesper_tc_pass_b": [_vp, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp],
 }
 
 

@@ -1,0 +1,287 @@
+// Search pass B on the 5th-generation tensor cores: the x-axis DFT of every
+// channel, the product with the conjugate target spectrum, the sum per score
+// group and the inverse x-axis DFT, as dense split-BF16 contractions with
+// float32 accumulation in TMEM (grids of side 32 and 64).
+//
+// Pass B of the FP32 search (k_pass_b, k_rpass_b) computes, for rotation b,
+// group g and column j = ky * H + kz of the (x, ky, kz) spectrum,
+//   U[b][g][x][j] = sum_k e^{+2 pi i k x / d} sum_{c in g} T[c][k][j] X_c[k][j],
+//   X_c[k][j] = sum_x e^{-2 pi i k x / d} S[b][c][x][j]          (T conjugated).
+// Here each column j is one row of an M = 128 tile (one TMEM lane), and a
+// length-d complex DFT is the real GEMM  X = A * B^T  with
+//   A[row][2x] = Re S, A[row][2x + 1] = Im S          (K = 2d),
+//   B[2k][2x] = cos t, B[2k][2x + 1] = sin t, B[2k + 1][2x] = -sin t,
+//   B[2k + 1][2x + 1] = cos t,  t = 2 pi (k x mod d) / d  (N = 2d).
+// The inverse uses the same matrix: IDFT(u) = conj(DFT(conj u)).
+//
+// Split-BF16: a float32 value v is held as hi = bf16(v), lo = bf16(v - hi);
+// each product is hi_a hi_b + hi_a lo_b + lo_a hi_b (three MMAs into one
+// float32 accumulator; lo_a lo_b, about 2^-16 of the product, is dropped).
+// The operands keep about 16 significant bits, so results carry relative errors
+// near 1e-5 of the line's magnitude, against near 1e-7 for the float32 FFT.
+//
+// One CTA = 128 threads = one M tile; thread t owns row t (TMEM lane t).  Per
+// channel: the CTA writes the split tile to shared memory, one thread issues
+// the 3 * K / 16 MMAs and commits them to an mbarrier, every thread reads its
+// row back with tcgen05.ld and accumulates the product in registers.  Waits
+// are bounded (200 ms of global time); a time-out sets *err, and the CTA waits
+// once more, frees its TMEM and returns.
+#include <cuda_bf16.h>
+
+#include <map>
+#include <mutex>
+#include <type_traits>
+
+#include "vesper_common.cuh"
+#define VG_PASS_TYPES_ONLY
+#include "vesper_passes.cuh"
+#include "vesper_tcdft.cuh"
+
+namespace vg {
+
+constexpr int kTcRows = 128;                     // M: columns j per CTA
+constexpr uint64_t kTcWaitNs = 200ull * 1000000; // bound on one mbarrier wait
+
+template <int D>
+struct TcGeom {
+    static constexpr int K = 2 * D;                                  // = N
+    static constexpr uint32_t SBO = (uint32_t)(K / 8) * 128;         // 8-row group stride
+    static constexpr size_t B_BYTES = (size_t)K * K * 2;             // one split of the DFT matrix
+    static constexpr size_t A_BYTES = (size_t)kTcRows * K * 2;       // one split of the tile
+    static constexpr uint32_t TMEM_COLS = K < 32 ? 32 : K;           // power of two for D = 32, 64
+    // + 64 bytes of barrier and TMEM slot, + 4 KB that no operand uses: every
+    // address an MMA could form from these descriptors stays inside the block
+    static constexpr size_t SMEM = 2 * B_BYTES + 2 * A_BYTES + 64 + 4096;
+};
+
+// The real-form DFT matrix, hi then lo, in the K-major core-matrix layout.
+template <int D>
+__global__ void k_tc_table(unsigned char *tab) {
+    constexpr int K = TcGeom<D>::K;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= K * K) return;
+    const int n = i / K, k = i % K;
+    const int kk = n >> 1, x = k >> 1;
+    const int m = (kk * x) % D;
+    double s, c;
+    sincospi(2.0 * (double)m / (double)D, &s, &c);
+    double v;
+    if ((n & 1) == 0) v = (k & 1) == 0 ? c : s;
+    else v = (k & 1) == 0 ? -s : c;
+    const __nv_bfloat16 hi = __double2bfloat16(v);
+    const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(hi));
+    const uint32_t off = tc::kmajor_off(n, k, K);
+    *(__nv_bfloat16 *)(tab + off) = hi;
+    *(__nv_bfloat16 *)(tab + TcGeom<D>::B_BYTES + off) = lo;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) {
+    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+// (re, im) of element x of this thread's row, split into the hi and lo tiles
+__device__ __forceinline__ void put_split(unsigned char *ah, unsigned char *al, int row, int x, int K, float re,
+                                          float im) {
+    const __nv_bfloat16 hr = __float2bfloat16_rn(re), hi_ = __float2bfloat16_rn(im);
+    const __nv_bfloat16 lr = __float2bfloat16_rn(re - __bfloat162float(hr));
+    const __nv_bfloat16 li = __float2bfloat16_rn(im - __bfloat162float(hi_));
+    const uint32_t off = tc::kmajor_off(row, 2 * x, K);
+    *(uint32_t *)(ah + off) = pack_bf16(hr, hi_);
+    *(uint32_t *)(al + off) = pack_bf16(lr, li);
+}
+
+// MMAs of one tile: D = A * B^T over K, split-BF16 (hi hi + hi lo + lo hi)
+template <int D>
+__device__ __forceinline__ void issue_split_mma(uint32_t tmem, const unsigned char *ah, const unsigned char *al,
+                                                const unsigned char *bh, const unsigned char *bl, uint64_t *mbar) {
+    using G = TcGeom<D>;
+    constexpr uint32_t idesc = tc::idesc_bf16(kTcRows, G::K);
+    const uint32_t sah = tc::smem_addr(ah), sal = tc::smem_addr(al);
+    const uint32_t sbh = tc::smem_addr(bh), sbl = tc::smem_addr(bl);
+#pragma unroll
+    for (int s = 0; s < G::K / 16; ++s) {
+        const uint32_t o = (uint32_t)s * 2 * tc::kLBO;
+        tc::mma_bf16(tmem, tc::smem_desc(sah + o, tc::kLBO, G::SBO), tc::smem_desc(sbh + o, tc::kLBO, G::SBO), idesc,
+                     s > 0 ? 1u : 0u);
+        tc::mma_bf16(tmem, tc::smem_desc(sah + o, tc::kLBO, G::SBO), tc::smem_desc(sbl + o, tc::kLBO, G::SBO), idesc,
+                     1u);
+        tc::mma_bf16(tmem, tc::smem_desc(sal + o, tc::kLBO, G::SBO), tc::smem_desc(sbh + o, tc::kLBO, G::SBO), idesc,
+                     1u);
+    }
+    tc::mma_commit(mbar);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kTcRows, 1) k_tcb(const PassB2 a, const unsigned char *tab, int *err) {
+    using G = TcGeom<D>;
+    constexpr int K = G::K;
+    constexpr int H = D / 2 + 1;
+    constexpr int dH = D * H;
+    extern __shared__ __align__(16) unsigned char smem[];   // 16-byte alignment suffices without swizzle
+    unsigned char *bh = smem, *bl = smem + G::B_BYTES;
+    unsigned char *ah = smem + 2 * G::B_BYTES, *al = ah + G::A_BYTES;
+    uint64_t *mbar = (uint64_t *)(al + G::A_BYTES);
+    uint32_t *tslot = (uint32_t *)(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int j = blockIdx.x * kTcRows + tid;
+    const int b = blockIdx.y;
+    const bool live = j < dH;
+
+    // the DFT matrix (hi, lo) into shared memory
+    {
+        const uint4 *src = (const uint4 *)tab;
+        uint4 *dst = (uint4 *)smem;
+        for (int i = tid; i < (int)(2 * G::B_BYTES / 16); i += kTcRows) dst[i] = __ldg(src + i);
+    }
+    if (tid == 0) tc::mbar_init(mbar, 1);
+    if (warp == 0) tc::tmem_alloc(tslot, G::TMEM_COLS);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
+    uint32_t phase = 0;
+    bool ok = true;
+
+    // one tile through the tensor core: write the rows, MMAs, wait; false on time-out
+    auto run_tile = [&]() -> bool {
+        tc::fence_smem_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            issue_split_mma<D>(tmem, ah, al, bh, bl, mbar);
+        }
+        const bool got = tc::mbar_wait(mbar, phase, kTcWaitNs);
+        phase ^= 1u;
+        tc::fence_after_sync();
+        return __syncthreads_and(got ? 1 : 0) != 0;
+    };
+
+    const float2 *S = a.S + (size_t)b * a.nch * D * dH;
+    float2 *U = a.U + (size_t)b * a.ngrp * D * dH;
+    for (int g = 0; g < a.ngrp && ok; ++g) {
+        const int cb = g == 0 ? 0 : a.split, ce = g == 0 ? (a.ngrp == 1 ? a.nch : a.split) : a.nch;
+        float ur[D], ui[D];
+#pragma unroll
+        for (int x = 0; x < D; ++x) ur[x] = ui[x] = 0.f;
+        for (int c = cb; c < ce && ok; ++c) {
+            const float2 *sc = S + (size_t)c * D * dH + j;
+#pragma unroll 8
+            for (int x = 0; x < D; ++x) {
+                const float2 v = live ? __ldg(sc + (size_t)x * dH) : make_float2(0.f, 0.f);
+                put_split(ah, al, tid, x, K, v.x, v.y);
+            }
+            ok = run_tile();
+            if (!ok) break;
+            // X_c[k] of this row, times the (conjugated) target spectrum, into the group sum
+            const float2 *tc_ = a.T + (size_t)c * D * dH + j;
+#pragma unroll
+            for (int q = 0; q < K / 16; ++q) {
+                float v[16];
+                tc::tmem_ld16(trow + (uint32_t)(q * 16), v);
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int k = q * 8 + e;
+                    const float2 t = live ? __ldg(tc_ + (size_t)k * dH) : make_float2(0.f, 0.f);
+                    ur[k] = fmaf(t.x, v[2 * e], fmaf(-t.y, v[2 * e + 1], ur[k]));
+                    ui[k] = fmaf(t.x, v[2 * e + 1], fmaf(t.y, v[2 * e], ui[k]));
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();   // every row read back before the next tile's MMAs
+        }
+        if (!ok) break;
+        // inverse DFT of the group sum: conj(DFT(conj u))
+#pragma unroll
+        for (int x = 0; x < D; ++x) put_split(ah, al, tid, x, K, ur[x], -ui[x]);
+        ok = run_tile();
+        if (!ok) break;
+        float2 *ug = U + (size_t)g * D * dH + j;
+#pragma unroll
+        for (int q = 0; q < K / 16; ++q) {
+            float v[16];
+            tc::tmem_ld16(trow + (uint32_t)(q * 16), v);
+            if (live) {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) ug[(size_t)(q * 8 + e) * dH] = make_float2(v[2 * e], -v[2 * e + 1]);
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+        // the MMAs of the timed-out tile may still run: wait for them once more
+        // (bounded) before the TMEM goes back
+        tc::mbar_wait(mbar, phase ^ 1u, kTcWaitNs);
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    if (warp == 0) tc::tmem_free(tmem, G::TMEM_COLS);
+}
+
+// ---- host ---------------------------------------------------------------------
+
+// the DFT table of side D on the current device, built on first use
+template <int D>
+static const unsigned char *tc_table(cudaStream_t st) {
+    static std::mutex mu;
+    static std::map<int, unsigned char *> tabs;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(mu);
+    auto it = tabs.find(dev);
+    if (it != tabs.end()) return it->second;
+    unsigned char *p = nullptr;
+    if (cudaMalloc(&p, 2 * TcGeom<D>::B_BYTES) != cudaSuccess) return nullptr;
+    constexpr int n = TcGeom<D>::K * TcGeom<D>::K;
+    k_tc_table<D><<<(n + 255) / 256, 256, 0, st>>>(p);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaFree(p);
+        return nullptr;
+    }
+    tabs[dev] = p;
+    return p;
+}
+
+bool tc_pass_b_supported(int d) { return d == 32 || d == 64; }
+
+// pass B of nb rotations on the tensor cores; err: device int, set to 1 when
+// a wait timed out (left untouched otherwise)
+int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st) {
+    if (nb < 1 || nb > 65535 || !err) return fail(VESPER_ERR_INVALID, "tc pass B: bad batch");
+    auto run = [&](auto dc) -> int {
+        constexpr int D = decltype(dc)::value;
+        const unsigned char *tab = tc_table<D>(st);
+        if (!tab) return cuda_check("tc pass B: DFT table");
+        constexpr size_t sm = TcGeom<D>::SMEM;
+        allow_smem(k_tcb<D>, sm);
+        const int dH = D * (D / 2 + 1);
+        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcRows, sm, st>>>(a, tab, err);
+        VG_CHECK_LAUNCH("k_tcb");
+        return VESPER_OK;
+    };
+    if (a.d == 32) return run(std::integral_constant<int, 32>{});
+    if (a.d == 64) return run(std::integral_constant<int, 64>{});
+    return fail(VESPER_ERR_UNSUPPORTED, "tc pass B: side %d (32 and 64 only)", a.d);
+}
+
+}  // namespace vg
+
+using namespace vg;
+
+extern "C" int vesper_tc_pass_b(const void *S, const void *T, void *U, int d, int nch, int ngrp, int split,
+                                int nbatch, int *err, void *stream) {
+    if (!S || !T || !U || !err || nch < 1 || ngrp < 1 || ngrp > 2 || split < 1 || split > nch)
+        return fail(VESPER_ERR_INVALID, "vesper_tc_pass_b: bad args");
+    if (ngrp == 2 && split >= nch) return fail(VESPER_ERR_INVALID, "vesper_tc_pass_b: empty second group");
+    PassB2 a{};
+    a.S = (const float2 *)S;
+    a.T = (const float2 *)T;
+    a.U = (float2 *)U;
+    a.d = d;
+    a.nch = nch;
+    a.ngrp = ngrp;
+    a.split = ngrp == 1 ? nch : split;
+    return tc_pass_b(a, nbatch, err, (cudaStream_t)stream);
+}
