@@ -163,9 +163,13 @@ int vesper_search(const void *spectra, const double *data, const float *vec, con
 /* vesper_search with explicit kernel choices, for the autotuner: HOST
  * opts[3] = {path (-1 automatic, 0 radix-stage passes, 1 register two-step
  * passes where compiled for this side and mode, 2 the fused single-kernel
- * search where compiled), channels per pass-A block (0 automatic), columns
- * per pass-B block (0 automatic)}.  Automatic picks 2, else 1, else 0.  Every
- * choice gives the same results up to float32 rounding of the FFT. */
+ * search where compiled, 3 pass B (x-axis DFTs, product, group sums) as
+ * split-BF16 tensor-core contractions with passes A and C as path 1, else 0;
+ * sides 32 and 64), channels per pass-A block (0 automatic), columns per
+ * pass-B block (0 automatic)}.  Automatic picks 2, else 1, else 0.  Paths
+ * 0-2 give the same results up to float32 rounding of the FFT; path 3 carries
+ * the split-BF16 error (about 1e-5 of a transform's magnitude).  After a path-3
+ * call, vesper_search_status reports whether a tensor-core wait timed out. */
 int vesper_search_tuned(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
                         int mode, double ave, const float *rotmats, int nrot, const double *mix, float *scores_out,
                         int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes, void *stream,
@@ -184,8 +188,14 @@ int vesper_search_profile(const void *spectra, const double *data, const float *
                           float *scores_out, int32_t *lin_out, int batch, void *workspace, size_t workspace_bytes,
                           void *stream, float *pass_ms, int *pass_launches, const int *opts);
 
+/* Status word of the last search that used this workspace (HOST *status_out:
+ * 0 ok, 1 a tensor-core pass timed out and its results are not valid).
+ * Synchronises the stream.  No counterpart in the reference. */
+int vesper_search_status(const void *workspace, size_t workspace_bytes, int *status_out, void *stream);
+
 /* Which kernel family vesper_search_tuned(opts) runs for this side and mode
- * (*path_out: 0 radix-stage, 1 register two-step, 2 fused) and how many
+ * (*path_out: 0 radix-stage, 1 register two-step, 2 fused, 3 tensor-core
+ * pass B) and how many
  * kernel launches it makes for nrot rotations at this batch (0: default).
  * No counterpart in the reference. */
 int vesper_search_plan(int dim, int mode, int batch, int nrot, const int *opts, int *path_out, int *launches_out);

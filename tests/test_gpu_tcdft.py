@@ -49,3 +49,78 @@ def test_tc_pass_b_matches_float64(dev, d, nch, ngrp, split):
     scale = np.max(np.abs(want))
     rel = np.max(np.abs(got - want)) / scale
     assert rel < 1e-4, rel
+
+
+def _fields(rng, d, zero_frac=0.6):
+    data = rng.uniform(0.1, 2.0, size=(d, d, d))
+    data[rng.random((d, d, d)) < zero_frac] = 0
+    vec = rng.normal(size=(d, d, d, 3))
+    vec /= np.linalg.norm(vec, axis=-1, keepdims=True)
+    vec[data == 0] = 0
+    probs = rng.dirichlet([0.5] * 4, size=(d, d, d)).astype(np.float32).transpose(3, 0, 1, 2).copy()
+    probs[:, data == 0] = 0
+    return data, vec.astype(np.float32), probs
+
+
+@pytest.mark.parametrize("d", [32, 64])
+def test_prob_search_tensor_pass_b_vs_fp64_oracle(dev, d):
+    """Prob-mode search with pass B on the tensor cores (path 3) and with the
+    float32 register passes (path 1), both against the float64 oracle: vector
+    and probability scores, and the mixed score.  Bars: path 1 as its own
+    test (1e-4, 1e-3); path 3 at 5e-4 and 5e-3 of the largest score (the
+    split-BF16 operands keep about 16 bits).  The measured errors are
+    printed."""
+    from oracle import vesper_oracle as orc
+    from vesper_python_gb300 import vesper as vg
+    rng = np.random.default_rng(100 + d)
+    tdata, tvec, tprobs = _fields(rng, d)
+    qdata, qvec, qprobs = _fields(rng, d)
+    angles = orc.calc_angle_comb(30.0)[::173]
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), "prob", 0.0, probs=dev.to_dev(tprobs),
+                                    dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(angles))
+    qd, qv, qp = dev.to_dev(qdata), dev.to_dev(qvec), dev.to_dev(qprobs)
+    tspec = orc.target_spectra([tvec[..., 0], tvec[..., 1], tvec[..., 2]] + list(tprobs))
+    ref = [orc.rot_and_search_prob(tspec, qdata, qvec, list(qprobs), a, 0.5, None, fp64=True) for a in angles]
+    rv = np.array([r[0] for r in ref])
+    rp = np.array([r[2] for r in ref])
+    st = orc.prob_stats(rv, rp, 1.0 / d ** 3)
+    mix = (0.5,) + tuple(st)
+    refm = np.array([orc.rot_and_search_prob(tspec, qdata, qvec, list(qprobs), a, 0.5, st, fp64=True)[4]
+                     for a in angles], np.float64)
+    assert vg.search_plan(d, "prob", opts=(3, 0, 0), dev=dev)[0] == 3
+    errs = {}
+    for path in (1, 3):
+        s1, _ = vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, dev=dev, opts=(path, 0, 0))
+        s2, _ = vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, mix=mix, dev=dev, opts=(path, 0, 0))
+        s1 = s1.cpu().numpy().astype(np.float64)
+        s2 = s2.cpu().numpy().astype(np.float64)
+        errs[path] = (np.max(np.abs(s1[:, 0] - rv)) / np.max(np.abs(rv)),
+                      np.max(np.abs(s1[:, 1] - rp)) / np.max(np.abs(rp)),
+                      np.max(np.abs(s2[:, 2] - refm)) / np.max(np.abs(refm)))
+    print(f"side {d}: relative errors (vec, prob, mixed) float32 path {errs[1]}, split-BF16 path {errs[3]}")
+    assert max(errs[1][:2]) < 1e-4 and errs[1][2] < 1e-3
+    assert max(errs[3][:2]) < 5e-4 and errs[3][2] < 5e-3
+
+
+def test_vec_search_tensor_pass_b_side32(dev):
+    """Mode V at side 32 with pass B on the tensor cores: scores against the
+    float32 path within 5e-4 of the largest, best translations equal except
+    where the two scores are that close."""
+    from oracle import vesper_oracle as orc
+    from vesper_python_gb300 import vesper as vg
+    d = 32
+    rng = np.random.default_rng(7)
+    tdata, tvec, _ = _fields(rng, d, 0.5)
+    qdata, qvec, _ = _fields(rng, d, 0.5)
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), "VecProduct", 0.0, dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(orc.calc_angle_comb(30.0)[::7]))
+    qd, qv = dev.to_dev(qdata), dev.to_dev(qvec)
+    sa, la = vg.search_device(spec, qd, qv, "VecProduct", 0.0, mats, dev=dev, opts=(1, 0, 0))
+    sb, lb = vg.search_device(spec, qd, qv, "VecProduct", 0.0, mats, dev=dev, opts=(3, 0, 0))
+    sa, sb = sa.cpu().numpy()[:, 0], sb.cpu().numpy()[:, 0]
+    scale = np.max(np.abs(sa))
+    assert np.max(np.abs(sa - sb)) < 5e-4 * scale
+    diff = la.cpu().numpy()[:, 0] != lb.cpu().numpy()[:, 0]
+    assert np.all(np.abs(sa - sb)[diff] < 5e-4 * scale)
+    assert int(diff.sum()) <= max(1, len(sa) // 50)

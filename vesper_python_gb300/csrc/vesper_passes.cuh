@@ -160,6 +160,10 @@ struct PassB2 {
     FftPlan P;
 };
 
+// pass B on the tensor cores (split-BF16 DFTs; vesper_tcdft.cu), sides 32 and 64
+bool tc_pass_b_supported(int d);
+int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st);
+
 __host__ __device__ inline size_t smem_b2(int d, int ntab, int nch, int ngrp, int W) {
     return smem_head(d, ntab) + (size_t)(nch + ngrp) * d * W * sizeof(float2);
 }

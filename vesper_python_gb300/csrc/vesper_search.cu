@@ -152,6 +152,7 @@ extern "C" int vesper_search_workspace_size(int dim, int mode, int batch, int nr
     if (batch <= 0) batch = default_batch(dim, mode);
     const size_t H = dim / 2 + 1, N = (size_t)dim * dim * dim;
     Carver cv(nullptr, 0);
+    cv.take<int>(64);   // status word (tensor-core pass B time-outs)
     cv.take<float4>(N);
     if (mode == VESPER_MODE_PROB) cv.take<float4>(N);
     cv.take<float2>((size_t)batch * mode_nch(mode) * dim * dim * H);
@@ -187,6 +188,10 @@ static int search_impl(const void *spectra, const double *data, const float *vec
     cfg.path = 0;
     const RegEntry *reg = find_reg(mode, dim);
     const int want_path = opts ? opts[0] : -1;
+    // path 3: pass B on the tensor cores (split-BF16), passes A and C as path 1 (else 0)
+    const bool tcb = want_path == 3;
+    if (tcb && !tc_pass_b_supported(dim))
+        return fail(VESPER_ERR_UNSUPPORTED, "tensor-core pass B: side %d (32 and 64 only)", dim);
     if (reg && want_path != 0) {
         const size_t lim = (size_t)smem_limit();
         const int nchr = mode_nch(mode), ngrr = mode_ngrp(mode);
@@ -223,10 +228,13 @@ static int search_impl(const void *spectra, const double *data, const float *vec
     if (want_path == 1 && cfg.path != 1)
         return fail(VESPER_ERR_UNSUPPORTED, "no register-FFT passes compiled for mode %d, side %d", mode, dim);
     cudaStream_t st = (cudaStream_t)stream;
+    if (tcb && cudaMemsetAsync(workspace, 0, sizeof(int), st) != cudaSuccess)
+        return cuda_check("vesper_search: status word");
     const int H = dim / 2 + 1, nch = mode_nch(mode), ngrp = mode_ngrp(mode);
     const size_t N = (size_t)dim * dim * dim;
     const int nscore = vesper_search_nscore(mode, mix != nullptr);
     Carver cv(workspace, workspace_bytes);
+    int *status = cv.take<int>(64);
     float4 *q4 = cv.take<float4>(N);
     float4 *p4 = mode == VESPER_MODE_PROB ? cv.take<float4>(N) : nullptr;
     float2 *S = cv.take<float2>((size_t)batch * nch * dim * dim * H);
@@ -308,8 +316,13 @@ static int search_impl(const void *spectra, const double *data, const float *vec
             VG_CHECK_LAUNCH("k_rpass_a");
             mark(0, 1);
             mark(1, 0);
-            reg->b(dim3(nbx, nb), kThreads, cfg.sb, st, pb);
-            VG_CHECK_LAUNCH("k_rpass_b");
+            if (tcb) {
+                rc = tc_pass_b(pb, nb, status, st);
+                if (rc) return rc;
+            } else {
+                reg->b(dim3(nbx, nb), kThreads, cfg.sb, st, pb);
+                VG_CHECK_LAUNCH("k_rpass_b");
+            }
             mark(1, 1);
             mark(2, 0);
             reg->c(gplane, kThreads, cfg.sc, st, pc, nscore);
@@ -329,8 +342,13 @@ static int search_impl(const void *spectra, const double *data, const float *vec
         VG_CHECK_LAUNCH("k_pass_a");
         mark(0, 1);
         mark(1, 0);
-        k_pass_b<<<dim3(nbx, nb), cfg.threads, cfg.sb, st>>>(pb);
-        VG_CHECK_LAUNCH("k_pass_b");
+        if (tcb) {
+            rc = tc_pass_b(pb, nb, status, st);
+            if (rc) return rc;
+        } else {
+            k_pass_b<<<dim3(nbx, nb), cfg.threads, cfg.sb, st>>>(pb);
+            VG_CHECK_LAUNCH("k_pass_b");
+        }
         mark(1, 1);
         mark(2, 0);
         switch (nscore) {
@@ -414,11 +432,27 @@ extern "C" int vesper_search_plan(int dim, int mode, int batch, int nrot, const 
     else if (want != 0 && want != 2 && find_reg(mode, dim))
         path = 1;
     if (want == 2 && path != 2) return fail(VESPER_ERR_UNSUPPORTED, "no fused search for mode %d, side %d", mode, dim);
+    if (want == 3) {
+        if (!tc_pass_b_supported(dim))
+            return fail(VESPER_ERR_UNSUPPORTED, "tensor-core pass B: side %d (32 and 64 only)", dim);
+        path = 3;
+    }
     if (batch <= 0) batch = default_batch(dim, mode);
     const int nb = nrot > 0 ? (nrot + batch - 1) / batch : 0;
     *path_out = path;
     // pack + passes (+ the gathered density of each Laplacian batch) + decode
     *launches_out = nrot > 0 ? 2 + (path == 2 ? 1 : (mode == VESPER_MODE_LAPLACIAN ? 4 : 3) * nb) : 0;
+    return VESPER_OK;
+}
+
+extern "C" int vesper_search_status(const void *workspace, size_t workspace_bytes, int *status_out, void *stream) {
+    if (!workspace || workspace_bytes < sizeof(int) || !status_out)
+        return fail(VESPER_ERR_INVALID, "vesper_search_status: bad args");
+    int v = 0;
+    if (cudaMemcpyAsync(&v, workspace, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream) != cudaSuccess ||
+        cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+        return cuda_check("vesper_search_status");
+    *status_out = v;
     return VESPER_OK;
 }
 

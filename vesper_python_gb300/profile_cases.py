@@ -12,7 +12,7 @@
   python -m vesper_python_gb300.profile_cases prob<d>
       prob-mode searches (both passes) of seeded random side-d fields with
       four probability channels over the 15-degree grid, timed per kernel
-      family
+      family (at sides 32 and 64 also with pass B on the tensor cores)
 
 Each run is a few GPU milliseconds, so a capture of one of its launches ends
 in seconds.
@@ -68,7 +68,10 @@ def main(argv=None):
         mats = vg.rot_matrices_device(vg.calc_angle_comb(15.0), dev, key=("grid", 15.0))
         n = int(mats.shape[0])
         mix = (0.5, 1.0, 0.0, 1.0, 0.0)
-        for path in ([0, 1] if vg.search_plan(d, "prob", dev=dev)[0] == 1 else [0]):
+        paths = [0, 1] if vg.search_plan(d, "prob", dev=dev)[0] == 1 else [0]
+        if d in (32, 64):
+            paths.append(3)       # pass B on the tensor cores (split-BF16)
+        for path in paths:
             for label, mx in (("pass1", None), ("pass2", mix)):
                 vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, mix=mx, dev=dev, opts=(path, 0, 0))
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -78,8 +81,12 @@ def main(argv=None):
                 e1.record()
                 torch.cuda.synchronize()
                 ms = e0.elapsed_time(e1) / 3
+                prof = {}
+                vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, mix=mx, dev=dev, opts=(path, 0, 0),
+                                 profile=prof)
+                passes = " / ".join(f"{1000 * t / n:.3f}" for t in prof["pass_ms"][:3])
                 print(f"prob side {d} path {path} {label}: {ms:.2f} ms for {n} rotations, "
-                      f"{1000 * ms / n:.3f} us per rotation")
+                      f"{1000 * ms / n:.3f} us per rotation (passes A / B / C {passes} us)")
     elif what == "fastvec":
         import contextlib
         import io
