@@ -20,13 +20,16 @@
 // The operands keep about 16 significant bits, so results carry relative errors
 // near 1e-5 of the line's magnitude, against near 1e-7 for the float32 FFT.
 //
-// One CTA = 128 threads = one M tile; thread t owns row t (TMEM lane t).  Per
-// channel: the CTA writes the split tile to shared memory, one thread issues
+// One CTA = one M tile of 128 rows, 256 threads: threads t and t + 128 own row
+// t (TMEM lane t), each half of its elements.  Per channel: a TMA box brings
+// the S lines to shared memory, the CTA writes the split tile, one thread issues
 // the 3 * K / 16 MMAs and commits them to an mbarrier, every thread reads its
 // row back with tcgen05.ld and accumulates the product in registers.  Waits
 // are bounded (200 ms of global time); a time-out sets *err, and the CTA waits
 // once more, frees its TMEM and returns.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <map>
 #include <mutex>
@@ -40,6 +43,7 @@
 namespace vg {
 
 constexpr int kTcRows = 128;                     // M: columns j per CTA
+constexpr int kTcThreads = 256;                  // two threads per row: each takes half of its elements
 constexpr uint64_t kTcWaitNs = 200ull * 1000000; // bound on one mbarrier wait
 
 template <int D>
@@ -49,9 +53,10 @@ struct TcGeom {
     static constexpr size_t B_BYTES = (size_t)K * K * 2;             // one split of the DFT matrix
     static constexpr size_t A_BYTES = (size_t)kTcRows * K * 2;       // one split of the tile
     static constexpr uint32_t TMEM_COLS = K < 32 ? 32 : K;           // power of two for D = 32, 64
-    // + 64 bytes of barrier and TMEM slot, + 4 KB that no operand uses: every
+    static constexpr size_t STAGE_BYTES = (size_t)D * kTcRows * 8;   // one TMA box: D x 128 complex
+    // + 64 bytes of barriers and TMEM slot, + 4 KB that no operand uses: every
     // address an MMA could form from these descriptors stays inside the block
-    static constexpr size_t SMEM = 2 * B_BYTES + 2 * A_BYTES + 64 + 4096;
+    static constexpr size_t SMEM = 2 * B_BYTES + 2 * A_BYTES + STAGE_BYTES + 64 + 4096;
 };
 
 // The real-form DFT matrix, hi then lo, in the K-major core-matrix layout.
@@ -112,7 +117,9 @@ __device__ __forceinline__ void issue_split_mma(uint32_t tmem, const unsigned ch
 }
 
 template <int D>
-__global__ void __launch_bounds__(kTcRows, 1) k_tcb(const PassB2 a, const unsigned char *tab, int *err) {
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_tcb(const PassB2 a, const unsigned char *tab, const __grid_constant__ CUtensorMap tmS,
+          const __grid_constant__ CUtensorMap tmT, int *err) {
     using G = TcGeom<D>;
     constexpr int K = G::K;
     constexpr int H = D / 2 + 1;
@@ -120,10 +127,14 @@ __global__ void __launch_bounds__(kTcRows, 1) k_tcb(const PassB2 a, const unsign
     extern __shared__ __align__(16) unsigned char smem[];   // 16-byte alignment suffices without swizzle
     unsigned char *bh = smem, *bl = smem + G::B_BYTES;
     unsigned char *ah = smem + 2 * G::B_BYTES, *al = ah + G::A_BYTES;
-    uint64_t *mbar = (uint64_t *)(al + G::A_BYTES);
-    uint32_t *tslot = (uint32_t *)(mbar + 1);
+    float2 *stage = (float2 *)(al + G::A_BYTES);            // [D][128]: one TMA box of S or T
+    uint64_t *mbar_mma = (uint64_t *)((unsigned char *)stage + G::STAGE_BYTES);
+    uint64_t *mbar_tma = mbar_mma + 1;
+    uint32_t *tslot = (uint32_t *)(mbar_mma + 2);
+    constexpr int DH2 = D / 2;                     // elements of a row per thread
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int j = blockIdx.x * kTcRows + tid;
+    const int row = tid & (kTcRows - 1), half = tid >> 7;   // warps w and w + 4 share TMEM lanes 32 (w % 4) ..
+    const int j0 = blockIdx.x * kTcRows, j = j0 + row;
     const int b = blockIdx.y;
     const bool live = j < dH;
 
@@ -131,74 +142,95 @@ __global__ void __launch_bounds__(kTcRows, 1) k_tcb(const PassB2 a, const unsign
     {
         const uint4 *src = (const uint4 *)tab;
         uint4 *dst = (uint4 *)smem;
-        for (int i = tid; i < (int)(2 * G::B_BYTES / 16); i += kTcRows) dst[i] = __ldg(src + i);
+        for (int i = tid; i < (int)(2 * G::B_BYTES / 16); i += kTcThreads) dst[i] = __ldg(src + i);
     }
-    if (tid == 0) tc::mbar_init(mbar, 1);
+    if (tid == 0) {
+        tc::mbar_init(mbar_mma, 1);
+        tc::mbar_init(mbar_tma, 1);
+    }
     if (warp == 0) tc::tmem_alloc(tslot, G::TMEM_COLS);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
-    uint32_t phase = 0;
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);   // this warp's 32 lanes
+    uint32_t pm = 0, pt = 0;   // phases of the MMA and TMA barriers
     bool ok = true;
 
-    // one tile through the tensor core: write the rows, MMAs, wait; false on time-out
-    auto run_tile = [&]() -> bool {
+    // one thread: a TMA box (D rows x 128 columns) into the stage
+    auto load_box = [&](const CUtensorMap *tm, int c2) {
+        tc::fence_smem_async();
+        tc::mbar_expect_tx(mbar_tma, (uint32_t)G::STAGE_BYTES);
+        tc::tma_load_3d(stage, tm, j0, 0, c2, mbar_tma);
+    };
+    auto wait_tma = [&]() -> bool {
+        const bool got = tc::mbar_wait(mbar_tma, pt, kTcWaitNs);
+        pt ^= 1u;
+        return got;
+    };
+    // the split tile is in shared memory: MMAs (one thread), then, if load_t,
+    // the target box into the stage while they run
+    auto run_mma = [&](bool load_t, int c) -> bool {
         tc::fence_smem_async();
         __syncthreads();
         if (tid == 0) {
             tc::fence_after_sync();
-            issue_split_mma<D>(tmem, ah, al, bh, bl, mbar);
+            issue_split_mma<D>(tmem, ah, al, bh, bl, mbar_mma);
+            if (load_t) load_box(&tmT, c);
         }
-        const bool got = tc::mbar_wait(mbar, phase, kTcWaitNs);
-        phase ^= 1u;
+        bool got = tc::mbar_wait(mbar_mma, pm, kTcWaitNs);
+        pm ^= 1u;
         tc::fence_after_sync();
+        if (load_t) got = wait_tma() && got;
         return __syncthreads_and(got ? 1 : 0) != 0;
     };
 
-    const float2 *S = a.S + (size_t)b * a.nch * D * dH;
     float2 *U = a.U + (size_t)b * a.ngrp * D * dH;
     for (int g = 0; g < a.ngrp && ok; ++g) {
         const int cb = g == 0 ? 0 : a.split, ce = g == 0 ? (a.ngrp == 1 ? a.nch : a.split) : a.nch;
-        float ur[D], ui[D];
+        float ur[DH2], ui[DH2];   // frequencies half * D/2 + [0, D/2) of this row
 #pragma unroll
-        for (int x = 0; x < D; ++x) ur[x] = ui[x] = 0.f;
+        for (int x = 0; x < DH2; ++x) ur[x] = ui[x] = 0.f;
         for (int c = cb; c < ce && ok; ++c) {
-            const float2 *sc = S + (size_t)c * D * dH + j;
+            // S[b][c][x][j0 .. j0 + 127] (columns past dH arrive as zeros)
+            if (tid == 0) load_box(&tmS, b * a.nch + c);
+            ok = __syncthreads_and(wait_tma() ? 1 : 0) != 0;
+            if (!ok) break;
 #pragma unroll 8
-            for (int x = 0; x < D; ++x) {
-                const float2 v = live ? __ldg(sc + (size_t)x * dH) : make_float2(0.f, 0.f);
-                put_split(ah, al, tid, x, K, v.x, v.y);
+            for (int xq = 0; xq < DH2; ++xq) {
+                const int x = half * DH2 + xq;
+                const float2 v = stage[x * kTcRows + row];
+                put_split(ah, al, row, x, K, v.x, v.y);
             }
-            ok = run_tile();
+            ok = run_mma(true, c);   // T[c][k][j0 ..] lands in the stage meanwhile
             if (!ok) break;
             // X_c[k] of this row, times the (conjugated) target spectrum, into the group sum
-            const float2 *tc_ = a.T + (size_t)c * D * dH + j;
 #pragma unroll
-            for (int q = 0; q < K / 16; ++q) {
+            for (int qq = 0; qq < K / 32; ++qq) {
+                const int q = half * (K / 32) + qq;
                 float v[16];
                 tc::tmem_ld16(trow + (uint32_t)(q * 16), v);
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    const int k = q * 8 + e;
-                    const float2 t = live ? __ldg(tc_ + (size_t)k * dH) : make_float2(0.f, 0.f);
-                    ur[k] = fmaf(t.x, v[2 * e], fmaf(-t.y, v[2 * e + 1], ur[k]));
-                    ui[k] = fmaf(t.x, v[2 * e + 1], fmaf(t.y, v[2 * e], ui[k]));
+                    const int kq = qq * 8 + e, k = q * 8 + e;
+                    const float2 t = stage[k * kTcRows + row];
+                    ur[kq] = fmaf(t.x, v[2 * e], fmaf(-t.y, v[2 * e + 1], ur[kq]));
+                    ui[kq] = fmaf(t.x, v[2 * e + 1], fmaf(t.y, v[2 * e], ui[kq]));
                 }
             }
             tc::fence_before_sync();
-            __syncthreads();   // every row read back before the next tile's MMAs
+            __syncthreads();   // rows read back and the stage free before the next box and MMAs
         }
         if (!ok) break;
         // inverse DFT of the group sum: conj(DFT(conj u))
 #pragma unroll
-        for (int x = 0; x < D; ++x) put_split(ah, al, tid, x, K, ur[x], -ui[x]);
-        ok = run_tile();
+        for (int kq = 0; kq < DH2; ++kq) put_split(ah, al, row, half * DH2 + kq, K, ur[kq], -ui[kq]);
+        ok = run_mma(false, 0);
         if (!ok) break;
         float2 *ug = U + (size_t)g * D * dH + j;
 #pragma unroll
-        for (int q = 0; q < K / 16; ++q) {
+        for (int qq = 0; qq < K / 32; ++qq) {
+            const int q = half * (K / 32) + qq;
             float v[16];
             tc::tmem_ld16(trow + (uint32_t)(q * 16), v);
             if (live) {
@@ -211,9 +243,10 @@ __global__ void __launch_bounds__(kTcRows, 1) k_tcb(const PassB2 a, const unsign
     }
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
-        // the MMAs of the timed-out tile may still run: wait for them once more
-        // (bounded) before the TMEM goes back
-        tc::mbar_wait(mbar, phase ^ 1u, kTcWaitNs);
+        // work of the timed-out step may still run: wait for both barriers
+        // once more (bounded) before the TMEM goes back
+        tc::mbar_wait(mbar_mma, pm ^ 1u, kTcWaitNs);
+        tc::mbar_wait(mbar_tma, pt ^ 1u, kTcWaitNs);
         tc::fence_before_sync();
         __syncthreads();
     }
@@ -246,6 +279,35 @@ static const unsigned char *tc_table(cudaStream_t st) {
 
 bool tc_pass_b_supported(int d) { return d == 32 || d == 64; }
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    return fn;
+}
+
+// [planes][D][dH] complex64 (8-byte elements) in boxes of 128 x D x 1; columns
+// past dH read as zeros
+static bool box_map(CUtensorMap *m, const void *base, int D, int dH, int planes) {
+    const auto fn = encode_tiled();
+    if (!fn || ((uintptr_t)base & 15u)) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)dH, (cuuint64_t)D, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)dH * 8, (cuuint64_t)D * dH * 8};
+    const cuuint32_t box[3] = {(cuuint32_t)kTcRows, (cuuint32_t)D, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void *>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // pass B of nb rotations on the tensor cores; err: device int, set to 1 when
 // a wait timed out (left untouched otherwise)
 int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st) {
@@ -257,7 +319,10 @@ int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st) {
         constexpr size_t sm = TcGeom<D>::SMEM;
         allow_smem(k_tcb<D>, sm);
         const int dH = D * (D / 2 + 1);
-        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcRows, sm, st>>>(a, tab, err);
+        CUtensorMap tmS, tmT;
+        if ((dH * 8) % 16 || !box_map(&tmS, a.S, D, dH, nb * a.nch) || !box_map(&tmT, a.T, D, dH, a.nch))
+            return fail(VESPER_ERR_CUDA, "tc pass B: tensor maps (driver entry point or alignment)");
+        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcThreads, sm, st>>>(a, tab, tmS, tmT, err);
         VG_CHECK_LAUNCH("k_tcb");
         return VESPER_OK;
     };

@@ -87,10 +87,12 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// try_wait: the thread may be suspended until the phase completes or a
+// system-dependent time limit passes (wakes on completion, unlike a sleep)
 __device__ __forceinline__ uint32_t mbar_test(uint64_t *mbar, uint32_t phase) {
     uint32_t done;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(done)
         : "r"(smem_addr(mbar)), "r"(phase)
@@ -108,8 +110,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase, uint64
         uint64_t t;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
         if (t - t0 > limit_ns) return false;
-        __nanosleep(64);
     }
+}
+
+// one arrival on the mbarrier plus the bytes a bulk copy will deliver
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// TMA: box (c0, c1, c2) of a 3-D tensor map into shared memory; completion
+// counted in bytes on the mbarrier
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int c0, int c1, int c2, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(dst)),
+        "l"((uint64_t)tmap), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(mbar))
+        : "memory");
 }
 
 // 16 consecutive float32 TMEM columns of this thread's lane (32x32b shape:

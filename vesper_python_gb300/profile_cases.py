@@ -6,6 +6,9 @@
   python -m vesper_python_gb300.profile_cases prop
       three learned-proposal scorings (committed weights) of one held-out
       128^3 / 64^3 pair at s = 3 over the 10-degree grid
+  python -m vesper_python_gb300.profile_cases tcb<d>
+      the split-BF16 tensor-core pass B alone on random side-d spectra
+      (prob layout, 16 rotations), timed
   python -m vesper_python_gb300.profile_cases fastvec
       fastVEC of both maps of the seed-0 128^3 / 64^3 generator pair at s = 3,
       g = 16 (the learned-proposal workload's maps), timed per map
@@ -87,6 +90,31 @@ def main(argv=None):
                 passes = " / ".join(f"{1000 * t / n:.3f}" for t in prof["pass_ms"][:3])
                 print(f"prob side {d} path {path} {label}: {ms:.2f} ms for {n} rotations, "
                       f"{1000 * ms / n:.3f} us per rotation (passes A / B / C {passes} us)")
+    elif what.startswith("tcb"):
+        # the tensor-core pass B alone (vesper_tc_pass_b) on random spectra of
+        # side d, prob-mode layout (7 channels, 2 groups), 16 rotations, 3 calls
+        import ctypes
+
+        from . import _native
+        d = int(what[3:])
+        H = d // 2 + 1
+        nb = 16
+        g = torch.Generator(device=dev.device).manual_seed(d)
+        S = torch.randn((nb, 7, d, d, H), dtype=torch.complex64, device=dev.device, generator=g)
+        T = torch.randn((7, d, d, H), dtype=torch.complex64, device=dev.device, generator=g)
+        U = torch.empty((nb, 2, d, d, H), dtype=torch.complex64, device=dev.device)
+        err = torch.zeros(1, dtype=torch.int32, device=dev.device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for i in range(4):
+            if i == 1:
+                e0.record()
+            _native.check(dev.lib.vesper_tc_pass_b(ctypes.c_void_p(S.data_ptr()), ctypes.c_void_p(T.data_ptr()),
+                                                   ctypes.c_void_p(U.data_ptr()), d, 7, 2, 3, nb,
+                                                   ctypes.c_void_p(err.data_ptr()), dev.stream))
+        e1.record()
+        torch.cuda.synchronize()
+        print(f"tensor pass B side {d}: {1000 * e0.elapsed_time(e1) / 3 / nb:.3f} us per rotation, "
+              f"status {int(err.item())}")
     elif what == "fastvec":
         import contextlib
         import io
