@@ -52,7 +52,7 @@ struct TcGeom {
     static constexpr uint32_t SBO = (uint32_t)(K / 8) * 128;         // 8-row group stride
     static constexpr size_t B_BYTES = (size_t)K * K * 2;             // one split of the DFT matrix
     static constexpr size_t A_BYTES = (size_t)kTcRows * K * 2;       // one split of the tile
-    static constexpr uint32_t TMEM_COLS = K < 32 ? 32 : K;           // power of two for D = 32, 64
+    static constexpr uint32_t TMEM_COLS = 2 * K;                     // two accumulator buffers (128 or 256)
     static constexpr size_t STAGE_BYTES = (size_t)D * kTcRows * 8;   // one TMA box: D x 128 complex
     // + 64 bytes of barriers and TMEM slot, + 4 KB that no operand uses: every
     // address an MMA could form from these descriptors stays inside the block
@@ -118,20 +118,19 @@ __device__ __forceinline__ void issue_split_mma(uint32_t tmem, const unsigned ch
 
 template <int D>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_tcb(const PassB2 a, const unsigned char *tab, const __grid_constant__ CUtensorMap tmS,
-          const __grid_constant__ CUtensorMap tmT, int *err) {
+    k_tcb(const PassB2 a, const unsigned char *tab, const __grid_constant__ CUtensorMap tmS, int *err) {
     using G = TcGeom<D>;
     constexpr int K = G::K;
     constexpr int H = D / 2 + 1;
     constexpr int dH = D * H;
+    constexpr int DH2 = D / 2;                     // elements of a row per thread
     extern __shared__ __align__(16) unsigned char smem[];   // 16-byte alignment suffices without swizzle
     unsigned char *bh = smem, *bl = smem + G::B_BYTES;
     unsigned char *ah = smem + 2 * G::B_BYTES, *al = ah + G::A_BYTES;
-    float2 *stage = (float2 *)(al + G::A_BYTES);            // [D][128]: one TMA box of S or T
+    float2 *stage = (float2 *)(al + G::A_BYTES);            // [D][128]: one TMA box of S
     uint64_t *mbar_mma = (uint64_t *)((unsigned char *)stage + G::STAGE_BYTES);
     uint64_t *mbar_tma = mbar_mma + 1;
     uint32_t *tslot = (uint32_t *)(mbar_mma + 2);
-    constexpr int DH2 = D / 2;                     // elements of a row per thread
     const int tid = threadIdx.x, warp = tid >> 5;
     const int row = tid & (kTcRows - 1), half = tid >> 7;   // warps w and w + 4 share TMEM lanes 32 (w % 4) ..
     const int j0 = blockIdx.x * kTcRows, j = j0 + row;
@@ -157,44 +156,71 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t pm = 0, pt = 0;   // phases of the MMA and TMA barriers
     bool ok = true;
 
-    // one thread: a TMA box (D rows x 128 columns) into the stage
-    auto load_box = [&](const CUtensorMap *tm, int c2) {
+    // Tiles of one CTA, in order: the channels of group 0, its inverse, then
+    // (two groups) the channels of group 1 and its inverse.  Tile t's MMAs
+    // accumulate in TMEM buffer t & 1.
+    const int n0 = a.ngrp == 1 ? a.nch : a.split;
+    const int ntiles = a.nch + a.ngrp;
+    auto is_inv = [&](int t) { return t == n0 || t == a.nch + 1; };
+    auto chan = [&](int t) { return t < n0 ? t : t - 1; };
+
+    auto load_s = [&](int t) {   // one thread: the S box of channel tile t into the stage
         tc::fence_smem_async();
         tc::mbar_expect_tx(mbar_tma, (uint32_t)G::STAGE_BYTES);
-        tc::tma_load_3d(stage, tm, j0, 0, c2, mbar_tma);
-    };
-    auto wait_tma = [&]() -> bool {
-        const bool got = tc::mbar_wait(mbar_tma, pt, kTcWaitNs);
-        pt ^= 1u;
-        return got;
-    };
-    // the split tile is in shared memory: MMAs (one thread), then, if load_t,
-    // the target box into the stage while they run
-    auto run_mma = [&](bool load_t, int c) -> bool {
-        tc::fence_smem_async();
-        __syncthreads();
-        if (tid == 0) {
-            tc::fence_after_sync();
-            issue_split_mma<D>(tmem, ah, al, bh, bl, mbar_mma);
-            if (load_t) load_box(&tmT, c);
-        }
-        bool got = tc::mbar_wait(mbar_mma, pm, kTcWaitNs);
-        pm ^= 1u;
-        tc::fence_after_sync();
-        if (load_t) got = wait_tma() && got;
-        return __syncthreads_and(got ? 1 : 0) != 0;
+        tc::tma_load_3d(stage, &tmS, j0, 0, b * a.nch + chan(t), mbar_tma);
     };
 
-    float2 *U = a.U + (size_t)b * a.ngrp * D * dH;
-    for (int g = 0; g < a.ngrp && ok; ++g) {
-        const int cb = g == 0 ? 0 : a.split, ce = g == 0 ? (a.ngrp == 1 ? a.nch : a.split) : a.nch;
-        float ur[DH2], ui[DH2];   // frequencies half * D/2 + [0, D/2) of this row
+    float ur[DH2], ui[DH2];   // group sum at frequencies half * D/2 + [0, D/2) of this row
 #pragma unroll
-        for (int x = 0; x < DH2; ++x) ur[x] = ui[x] = 0.f;
-        for (int c = cb; c < ce && ok; ++c) {
-            // S[b][c][x][j0 .. j0 + 127] (columns past dH arrive as zeros)
-            if (tid == 0) load_box(&tmS, b * a.nch + c);
-            ok = __syncthreads_and(wait_tma() ? 1 : 0) != 0;
+    for (int x = 0; x < DH2; ++x) ur[x] = ui[x] = 0.f;
+    float2 *U = a.U + (size_t)b * a.ngrp * D * dH;
+
+    // read-back of tile t (its MMAs have completed): a channel's spectrum times
+    // the conjugate target into the group sum, or an inverse into U
+    auto epilogue = [&](int t) {
+        const uint32_t tb = trow + (uint32_t)((t & 1) * K);
+        if (!is_inv(t)) {
+            const float2 *tc_ = a.T + (size_t)chan(t) * D * dH + j;
+#pragma unroll
+            for (int qq = 0; qq < K / 32; ++qq) {
+                const int q = half * (K / 32) + qq;
+                float2 tv[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e)
+                    tv[e] = live ? __ldg(tc_ + (size_t)(q * 8 + e) * dH) : make_float2(0.f, 0.f);
+                float v[16];
+                tc::tmem_ld16(tb + (uint32_t)(q * 16), v);
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int kq = qq * 8 + e;
+                    ur[kq] = fmaf(tv[e].x, v[2 * e], fmaf(-tv[e].y, v[2 * e + 1], ur[kq]));
+                    ui[kq] = fmaf(tv[e].x, v[2 * e + 1], fmaf(tv[e].y, v[2 * e], ui[kq]));
+                }
+            }
+        } else {
+            float2 *ug = U + (size_t)(t == n0 ? 0 : 1) * D * dH + j;
+#pragma unroll
+            for (int qq = 0; qq < K / 32; ++qq) {
+                const int q = half * (K / 32) + qq;
+                float v[16];
+                tc::tmem_ld16(tb + (uint32_t)(q * 16), v);
+                if (live) {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        ug[(size_t)(q * 8 + e) * dH] = make_float2(v[2 * e], -v[2 * e + 1]);
+                }
+            }
+        }
+        tc::fence_before_sync();
+    };
+
+    if (tid == 0) load_s(0);
+    int pending = -1;   // tile whose read-back is still to do
+    for (int t = 0; t < ntiles && ok; ++t) {
+        if (!is_inv(t)) {
+            const bool got = tc::mbar_wait(mbar_tma, pt, kTcWaitNs);
+            pt ^= 1u;
+            ok = __syncthreads_and(got ? 1 : 0) != 0;
             if (!ok) break;
 #pragma unroll 8
             for (int xq = 0; xq < DH2; ++xq) {
@@ -202,54 +228,42 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const float2 v = stage[x * kTcRows + row];
                 put_split(ah, al, row, x, K, v.x, v.y);
             }
-            ok = run_mma(true, c);   // T[c][k][j0 ..] lands in the stage meanwhile
-            if (!ok) break;
-            // X_c[k] of this row, times the (conjugated) target spectrum, into the group sum
-#pragma unroll
-            for (int qq = 0; qq < K / 32; ++qq) {
-                const int q = half * (K / 32) + qq;
-                float v[16];
-                tc::tmem_ld16(trow + (uint32_t)(q * 16), v);
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int kq = qq * 8 + e, k = q * 8 + e;
-                    const float2 t = stage[k * kTcRows + row];
-                    ur[kq] = fmaf(t.x, v[2 * e], fmaf(-t.y, v[2 * e + 1], ur[kq]));
-                    ui[kq] = fmaf(t.x, v[2 * e + 1], fmaf(t.y, v[2 * e], ui[kq]));
-                }
+        } else {
+            if (pending >= 0) {   // the group sum needs the last channel's read-back
+                epilogue(pending);
+                pending = -1;
             }
-            tc::fence_before_sync();
-            __syncthreads();   // rows read back and the stage free before the next box and MMAs
-        }
-        if (!ok) break;
-        // inverse DFT of the group sum: conj(DFT(conj u))
+            // inverse DFT of the group sum: conj(DFT(conj u))
 #pragma unroll
-        for (int kq = 0; kq < DH2; ++kq) put_split(ah, al, row, half * DH2 + kq, K, ur[kq], -ui[kq]);
-        ok = run_mma(false, 0);
-        if (!ok) break;
-        float2 *ug = U + (size_t)g * D * dH + j;
-#pragma unroll
-        for (int qq = 0; qq < K / 32; ++qq) {
-            const int q = half * (K / 32) + qq;
-            float v[16];
-            tc::tmem_ld16(trow + (uint32_t)(q * 16), v);
-            if (live) {
-#pragma unroll
-                for (int e = 0; e < 8; ++e) ug[(size_t)(q * 8 + e) * dH] = make_float2(v[2 * e], -v[2 * e + 1]);
+            for (int kq = 0; kq < DH2; ++kq) {
+                put_split(ah, al, row, half * DH2 + kq, K, ur[kq], -ui[kq]);
+                ur[kq] = ui[kq] = 0.f;
             }
         }
-        tc::fence_before_sync();
+        tc::fence_smem_async();
         __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            issue_split_mma<D>(tmem + (uint32_t)((t & 1) * K), ah, al, bh, bl, mbar_mma);
+            if (t + 1 < ntiles && !is_inv(t + 1)) load_s(t + 1);   // the stage was read above
+        }
+        if (pending >= 0) epilogue(pending);   // overlaps this tile's MMAs
+        pending = t;
+        const bool got = tc::mbar_wait(mbar_mma, pm, kTcWaitNs);
+        pm ^= 1u;
+        tc::fence_after_sync();
+        ok = __syncthreads_and(got ? 1 : 0) != 0;   // MMAs done: the operand tile is free
     }
+    if (ok && pending >= 0) epilogue(pending);
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
         // work of the timed-out step may still run: wait for both barriers
         // once more (bounded) before the TMEM goes back
         tc::mbar_wait(mbar_mma, pm ^ 1u, kTcWaitNs);
         tc::mbar_wait(mbar_tma, pt ^ 1u, kTcWaitNs);
-        tc::fence_before_sync();
-        __syncthreads();
     }
+    tc::fence_before_sync();
+    __syncthreads();
     if (warp == 0) tc::tmem_free(tmem, G::TMEM_COLS);
 }
 
@@ -319,10 +333,10 @@ int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st) {
         constexpr size_t sm = TcGeom<D>::SMEM;
         allow_smem(k_tcb<D>, sm);
         const int dH = D * (D / 2 + 1);
-        CUtensorMap tmS, tmT;
-        if ((dH * 8) % 16 || !box_map(&tmS, a.S, D, dH, nb * a.nch) || !box_map(&tmT, a.T, D, dH, a.nch))
-            return fail(VESPER_ERR_CUDA, "tc pass B: tensor maps (driver entry point or alignment)");
-        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcThreads, sm, st>>>(a, tab, tmS, tmT, err);
+        CUtensorMap tmS;
+        if ((dH * 8) % 16 || !box_map(&tmS, a.S, D, dH, nb * a.nch))
+            return fail(VESPER_ERR_CUDA, "tc pass B: tensor map (driver entry point or alignment)");
+        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcThreads, sm, st>>>(a, tab, tmS, err);
         VG_CHECK_LAUNCH("k_tcb");
         return VESPER_OK;
     };
