@@ -57,7 +57,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=WORKLOAD, choices=["prop128_s3_a10", "pair200_s2_a10", "uneven64_s4_a15"])
+    ap.add_argument("--workload", default=WORKLOAD,
+                    choices=["prop128_s3_a10", "pair200_s2_a10", "uneven64_s4_a15", "prob128_s3_a15"])
     ap.add_argument("--pairs", type=int, default=16, help="pairs per step (prop128_s3_a10)")
     ap.add_argument("--mode", default="V", choices=list("VOCPL"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -494,6 +495,115 @@ def run_uneven(args):
     print(json.dumps(line), flush=True)
 
 
+def run_prob(args):
+    """prob128_s3_a15: one 128^3 / 64^3 pair with four probability channels
+    per step (Dirichlet(0.5) inside the thresholded density, rotated with map2),
+    s = 3, grids padded to 64^3, A = 15 (7,488 rotations), alpha = 0.5.  A step
+    is the prob-mode alignment on the device: fastVEC of the two densities and
+    the eight probability maps, target spectra, the statistics pass and the
+    mixed pass over the grid, top-N, and the mixed pass over the refinement
+    set.  Timed with the float32 pass B (headline) and with the split-BF16
+    tensor-core pass B (search path 3); the line reports both and how far the
+    split-BF16 scores are from the float32 ones."""
+    import contextlib
+    import io
+
+    import torch
+
+    from vesper_python_gb300 import synth
+    from vesper_python_gb300 import vesper as vg
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = vg.Device(f"cuda:{local}")
+    w = synth.WORKLOADS["prob128_s3_a15"]
+    pr = synth.workload_pair("prob128_s3_a15", seed=rank)
+    d, s_, g = int(w["pad"]), float(w["s"]), float(w["g"])
+    geo = []
+    for src, orig, th in ((pr.map1, pr.orig1, w["t"]), (pr.map2, pr.orig2, w["T"])):
+        m = vg.mrc_obj.from_array(src, 1.0, orig)
+        with contextlib.redirect_stdout(io.StringIO()):
+            _, mn = vg.mrc_set_vox_size(m, th, s_)
+        geo.append((dev.to_dev(m.data), np.float64(m.xwidth), m.orig.astype(np.float64),
+                    np.asarray(mn.cent, np.float64) - 0.5 * s_ * d))
+    pmaps = [[dev.to_dev(np.ascontiguousarray(pm[..., k], np.float32)) for k in range(4)]
+             for pm in (pr.prob1, pr.prob2)]
+    angles = vg.calc_angle_comb(w["A"])
+    mats = vg.rot_matrices_device(angles, dev, key=("grid", float(w["A"])))
+    n = len(angles)
+    rd3 = 1.0 / d ** 3
+    alpha = float(w["alpha"])
+
+    def fields(i):
+        # prob mode keeps fastVEC's density in float32 (main.py:345)
+        src, sw, so, no = geo[i]
+        _, d32, vec = vg.fastvec_device(src, sw, so, d, s_, no, g, dev=dev)
+        probs = torch.stack([vg.fastvec_device(pm, sw, so, d, s_, no, g, dev=dev)[1] for pm in pmaps[i]])
+        return d32.double(), vec, probs
+
+    def step(path):
+        opts = (path, 0, 0)
+        tdata, tvec, tprobs = fields(0)
+        qdata, qvec, qprobs = fields(1)
+        spec = vg.target_spectra_device(tdata, tvec, "prob", 0.0, probs=tprobs, dev=dev)
+        s1, _ = vg.search_device(spec, qdata, qvec, "prob", 0.0, mats, probs=qprobs, dev=dev, opts=opts)
+        h = s1.cpu().numpy().astype(np.float64) * rd3
+        mix = (alpha, float(np.std(h[:, 0])), float(np.mean(h[:, 0])), float(np.std(h[:, 1])),
+               float(np.mean(h[:, 1])))
+        s2, l2 = vg.search_device(spec, qdata, qvec, "prob", 0.0, mats, probs=qprobs, mix=mix, dev=dev, opts=opts)
+        top = [int(t) for t in vg.topn_device(s2, w["N"], column=2, dev=dev).cpu().numpy() if t >= 0]
+        ref = vg.refine_angle_list([angles[t] for t in top])
+        rs, rl = vg.search_device(spec, qdata, qvec, "prob", 0.0, dev.to_dev(vg.rot_matrices(ref)), probs=qprobs,
+                                  mix=mix, dev=dev, opts=opts)
+        rtop = [int(t) for t in vg.topn_device(rs, w["N"], column=2, dev=dev).cpu().numpy() if t >= 0]
+        return s1, s2, top, rtop
+
+    out = {}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev.device)
+    for path in (-1, 3):
+        for _ in range(args.warmup):
+            res = step(path)
+        torch.cuda.synchronize()
+        clk = ClockSampler(local)
+        clk.start()
+        total = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            res = step(path)
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        out[path] = (total / args.steps, res, clk.stop())
+    ms, (s1, s2, top, rtop), clocks = out[-1]
+    ms3, (t1, t2, ttop, trtop), _ = out[3]
+    a1, b1 = s1.cpu().numpy().astype(np.float64), t1.cpu().numpy().astype(np.float64)
+    a2, b2 = s2.cpu().numpy().astype(np.float64), t2.cpu().numpy().astype(np.float64)
+    rel = lambda x, y: float(np.max(np.abs(x - y)) / max(np.max(np.abs(x)), 1e-300))
+    line = {
+        "metric": "prob-mode map-pair alignments/s", "value": round(1e3 / ms, 4), "unit": "alignments/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 FFT (f64 target spectra); split-BF16 pass B in the comparison",
+        "data": "synthetic (seeded 128^3 / 64^3 blob-map pair at 1 A, 4 Dirichlet(0.5) probability channels)",
+        "config": {"workload": f"prob128_s3_a15: one pair per step, s={s_}, grids padded to {d}^3, A={w['A']} "
+                               f"({n} rotations, statistics pass + mixed pass) + refinement, alpha={alpha}, "
+                               f"g={g}, N={w['N']}; fastVEC of the densities and the 8 probability maps in the step",
+                   "grid_side": d, "l2": "flushed before every step (256 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "split_bf16_pass_b": {"value": round(1e3 / ms3, 4), "ms_per_step": round(ms3, 3),
+                              "max_rel_diff_vs_f32": {"vec_score": rel(a1[:, 0], b1[:, 0]),
+                                                      "prob_score": rel(a1[:, 1], b1[:, 1]),
+                                                      "mixed_score": rel(a2[:, 2], b2[:, 2])},
+                              "top_n_same": top == ttop, "refined_top_n_same": rtop == trtop},
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+
+
 def cpu_baseline(args, threads, budget_s):
     """The reference algorithm on this host's CPU (the oracle restatement,
     exhaustive search like the reference), timed on a bounded sample and
@@ -576,5 +686,7 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.workload == "uneven64_s4_a15":
         run_uneven(a)
+    elif a.workload == "prob128_s3_a15":
+        run_prob(a)
     else:
         run_gb300(a)
