@@ -60,3 +60,28 @@ def test_invalid_arguments_return_status():
     rc = lib.vesper_fastvec(None, 1, 1, 1, 1.0, None, 4, 1.0, None, 16.0, None, None, None, None, 0, None)
     assert rc == 1
     assert lib.vesper_search_workspace_size(12, 0, 0, 10, ctypes.POINTER(ctypes.c_size_t)()) == 1
+
+
+def test_tensor_core_path_host_checks():
+    """Search path 3 (split-BF16 pass B): the plan reports it at sides 32 and
+    64 and refuses other sides; the pass-B entry validates its arguments
+    before touching the GPU."""
+    lib = _native.load()
+    path, nl = ctypes.c_int(-9), ctypes.c_int(-9)
+    opts = (ctypes.c_int * 3)(3, 0, 0)
+    for d in (32, 64):
+        assert lib.vesper_search_plan(d, 5, 8, 100, opts, ctypes.byref(path), ctypes.byref(nl)) == 0
+        assert path.value == 3 and nl.value == 2 + 3 * 13
+    assert lib.vesper_search_plan(30, 5, 8, 100, opts, ctypes.byref(path), ctypes.byref(nl)) == 2
+    # bad channel split, empty second group, unsupported side
+    assert lib.vesper_tc_pass_b(None, None, None, 64, 7, 2, 3, 1, None, None) == 1
+    assert lib.vesper_tc_pass_b(1, 1, 1, 64, 3, 2, 3, 1, 1, None) == 1
+    assert lib.vesper_tc_pass_b(1, 1, 1, 30, 3, 1, 3, 1, 1, None) == 2
+    assert lib.vesper_search_status(None, 0, None, None) == 1
+
+
+def test_topk_subset_batch_rejects_bad_args():
+    lib = _native.load()
+    assert lib.vesper_topk_subset_batch(None, 2, 100, 5, None, None) == 1
+    assert lib.vesper_topk_subset_batch(1, 0, 100, 5, 1, None) == 1
+    assert lib.vesper_topk_subset_batch(1, 2, 100, 101, 1, None) == 1

@@ -193,3 +193,28 @@ def test_model_translation_is_convert_trans():
     want = orc.convert_trans(np.array([10.0, 20.0, 30.0]), np.array([5.0, 6.0, 7.0]),
                              orc.euler2rot((30.0, 60.0, 90.0)), (3, 20, 1), 3.0, 24)
     assert np.array_equal(m.translation, want)
+
+
+def test_distinct_lattice_rows_expand_back():
+    """Refinement sets searched once per distinct angle: every entry of every
+    pair's list maps back to its own lattice row within its pair's block."""
+    from vesper_python_gb300 import align
+    from vesper_python_gb300 import vesper as vg
+    ac = vg.calc_angle_comb(10.0)
+    rng = np.random.default_rng(4)
+    sets = []
+    for _ in range(5):   # clustered top-N (many overlaps) and scattered ones
+        base = int(rng.integers(0, len(ac) - 1300))
+        sets.append(vg.refine_angle_list([ac[base + o] for o in (0, 1, 36, 37, 1296, 2, 3, 38, 72, 1297)]))
+        sets.append(vg.refine_angle_list([ac[i] for i in rng.integers(0, len(ac), 10)]))
+    key = vg.lattice_index(np.concatenate(sets))
+    rows, counts, local = align.distinct_lattice_rows(key, [len(s) for s in sets])
+    assert counts.sum() == len(rows) and len(local) == len(key)
+    off = ioff = 0
+    for s, c in zip(sets, counts):
+        blk = rows[off:off + c]
+        assert np.all(np.diff(blk) > 0)          # distinct within the pair
+        assert np.array_equal(blk[local[ioff:ioff + len(s)]], vg.lattice_index(s))
+        off += c
+        ioff += len(s)
+    assert counts[0] < len(sets[0])              # the clustered set repeats angles

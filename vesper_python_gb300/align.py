@@ -82,6 +82,20 @@ _NP_DTYPES = {torch.float32: np.dtype(np.float32), torch.float64: np.dtype(np.fl
               torch.uint8: np.dtype(np.uint8)}
 
 
+def distinct_lattice_rows(key, lens):
+    """Distinct lattice rows of consecutive angle lists (list i has lens[i]
+    entries; key = their lattice rows, concatenated): the distinct rows pair by
+    pair (ascending within a pair), their count per pair, and for every entry
+    its position within its pair's distinct rows."""
+    lens = np.asarray(lens, np.int64)
+    span = vg.LATTICE_N ** 3
+    pid = np.repeat(np.arange(len(lens), dtype=np.int64), lens)
+    ukeys, inv = np.unique(pid * span + np.asarray(key, np.int64), return_inverse=True)
+    counts = np.bincount(ukeys // span, minlength=len(lens))
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    return ukeys % span, counts, inv.reshape(-1) - starts[pid]
+
+
 def _size_grid(dmax2_bits, count, cent, width, orig, s):
     """mrc_set_vox_size (VESPER_1_prob_new.py:81-100) from the device radius."""
     if count == 0:
@@ -355,14 +369,9 @@ class Aligner:
             allm = vg.rot_matrices_lattice(np.concatenate([u for u, _ in uniq]), dev)
             inv = np.concatenate([iv.reshape(-1) for _, iv in uniq]).astype(np.int64)
             return allm, [len(u) for u, _ in uniq], dev.to_dev_async(inv)
-        span = vg.LATTICE_N ** 3
-        pid = np.repeat(np.arange(len(sets), dtype=np.int64), lens)
-        ukeys, inv = np.unique(pid * span + key, return_inverse=True)
-        upid = ukeys // span
-        counts = np.bincount(upid, minlength=len(sets))
-        starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
-        allm = vg.lattice_rot_matrices_device(dev).index_select(0, dev.to_dev_async(ukeys % span))
-        return allm, [int(c) for c in counts], dev.to_dev_async(inv.reshape(-1) - starts[pid])
+        rows, counts, local = distinct_lattice_rows(key, lens)
+        allm = vg.lattice_rot_matrices_device(dev).index_select(0, dev.to_dev_async(rows))
+        return allm, [int(c) for c in counts], dev.to_dev_async(local)
 
     FV_STREAMS = 4
 
