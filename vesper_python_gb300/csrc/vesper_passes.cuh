@@ -162,6 +162,7 @@ struct PassB2 {
 
 // pass B on the tensor cores (split-BF16 DFTs; vesper_tcdft.cu), sides 32 and 64
 bool tc_pass_b_supported(int d);
+int tc_pass_b_wave(int d);   // rotations per full wave of its CTAs
 int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st);
 
 __host__ __device__ inline size_t smem_b2(int d, int ntab, int nch, int ngrp, int W) {

@@ -230,6 +230,10 @@ static int search_impl(const void *spectra, const double *data, const float *vec
     cudaStream_t st = (cudaStream_t)stream;
     if (tcb && cudaMemsetAsync(workspace, 0, sizeof(int), st) != cudaSuccess)
         return cuda_check("vesper_search: status word");
+    if (tcb) {   // batches of whole waves of tensor-core CTAs (a partial extra wave costs a full one)
+        const int wave = tc_pass_b_wave(dim);
+        if (batch > wave) batch = batch / wave * wave;
+    }
     const int H = dim / 2 + 1, nch = mode_nch(mode), ngrp = mode_ngrp(mode);
     const size_t N = (size_t)dim * dim * dim;
     const int nscore = vesper_search_nscore(mode, mix != nullptr);
@@ -438,6 +442,10 @@ extern "C" int vesper_search_plan(int dim, int mode, int batch, int nrot, const 
         path = 3;
     }
     if (batch <= 0) batch = default_batch(dim, mode);
+    if (path == 3) {   // as the search does: batches of whole waves of tensor-core CTAs
+        const int wave = tc_pass_b_wave(dim);
+        if (batch > wave) batch = batch / wave * wave;
+    }
     const int nb = nrot > 0 ? (nrot + batch - 1) / batch : 0;
     *path_out = path;
     // pack + passes (+ the gathered density of each Laplacian batch) + decode

@@ -180,21 +180,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     auto epilogue = [&](int t) {
         const uint32_t tb = trow + (uint32_t)((t & 1) * K);
         if (!is_inv(t)) {
-            const float2 *tc_ = a.T + (size_t)chan(t) * D * dH + j;
+            // this thread's D/2 target values first: one L2 round trip for all
+            const float2 *tc_ = a.T + (size_t)chan(t) * D * dH + (size_t)half * DH2 * dH + j;
+            float2 tv[DH2];
+#pragma unroll
+            for (int kq = 0; kq < DH2; ++kq) tv[kq] = live ? __ldg(tc_ + (size_t)kq * dH) : make_float2(0.f, 0.f);
 #pragma unroll
             for (int qq = 0; qq < K / 32; ++qq) {
                 const int q = half * (K / 32) + qq;
-                float2 tv[8];
-#pragma unroll
-                for (int e = 0; e < 8; ++e)
-                    tv[e] = live ? __ldg(tc_ + (size_t)(q * 8 + e) * dH) : make_float2(0.f, 0.f);
                 float v[16];
                 tc::tmem_ld16(tb + (uint32_t)(q * 16), v);
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int kq = qq * 8 + e;
-                    ur[kq] = fmaf(tv[e].x, v[2 * e], fmaf(-tv[e].y, v[2 * e + 1], ur[kq]));
-                    ui[kq] = fmaf(tv[e].x, v[2 * e + 1], fmaf(tv[e].y, v[2 * e], ui[kq]));
+                    ur[kq] = fmaf(tv[kq].x, v[2 * e], fmaf(-tv[kq].y, v[2 * e + 1], ur[kq]));
+                    ui[kq] = fmaf(tv[kq].x, v[2 * e + 1], fmaf(tv[kq].y, v[2 * e], ui[kq]));
                 }
             }
         } else {
@@ -292,6 +292,20 @@ static const unsigned char *tc_table(cudaStream_t st) {
 }
 
 bool tc_pass_b_supported(int d) { return d == 32 || d == 64; }
+
+// rotations per full wave of pass-B CTAs on this device (column tiles of 128
+// per rotation; CTAs resident per SM by shared memory), at least 1
+int tc_pass_b_wave(int d) {
+    if (!tc_pass_b_supported(d)) return 1;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) return 1;
+    const size_t sm = d == 32 ? TcGeom<32>::SMEM : TcGeom<64>::SMEM;
+    const int per_sm = std::max(1, (int)((size_t)smem_limit() / (sm + 1024)));
+    const int dH = d * (d / 2 + 1);
+    const int tiles = (dH + kTcRows - 1) / kTcRows;
+    return std::max(1, nsm * per_sm / tiles);
+}
 
 // cuTensorMapEncodeTiled from the driver, looked up once through the runtime
 static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {

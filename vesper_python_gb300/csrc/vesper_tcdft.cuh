@@ -132,6 +132,9 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int c0,
 // 16 consecutive float32 TMEM columns of this thread's lane (32x32b shape:
 // warp w of the CTA reads lanes 32w .. 32w + 31).  The load and its wait are
 // one asm statement, so no use of the registers can be scheduled between them.
+// No memory clobber: TMEM is not memory the compiler orders, so independent
+// global and shared loads may be scheduled across it (ordering against the
+// MMAs comes from the mbarrier wait and tcgen05 fences, which do clobber).
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];
     asm volatile(
@@ -140,8 +143,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
         "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
+        : "r"(taddr));
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
