@@ -84,15 +84,28 @@ __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) 
     return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
-// (re, im) of element x of this thread's row, split into the hi and lo tiles
-__device__ __forceinline__ void put_split(unsigned char *ah, unsigned char *al, int row, int x, int K, float re,
-                                          float im) {
+// (re, im) split into packed hi and lo bf16 pairs (re in the low half)
+__device__ __forceinline__ void split_pair(float re, float im, uint32_t &h, uint32_t &l) {
     const __nv_bfloat16 hr = __float2bfloat16_rn(re), hi_ = __float2bfloat16_rn(im);
     const __nv_bfloat16 lr = __float2bfloat16_rn(re - __bfloat162float(hr));
     const __nv_bfloat16 li = __float2bfloat16_rn(im - __bfloat162float(hi_));
-    const uint32_t off = tc::kmajor_off(row, 2 * x, K);
-    *(uint32_t *)(ah + off) = pack_bf16(hr, hi_);
-    *(uint32_t *)(al + off) = pack_bf16(lr, li);
+    h = pack_bf16(hr, hi_);
+    l = pack_bf16(lr, li);
+}
+
+// elements x0 .. x0 + 3 (x0 a multiple of 4) of this thread's row into the hi
+// and lo tiles: one 16-byte chunk of a core-matrix row each, so eight rows of a
+// warp fill one 128-byte shared-memory wavefront
+__device__ __forceinline__ void put_split4(unsigned char *ah, unsigned char *al, int row, int x0, int K, float2 v0,
+                                           float2 v1, float2 v2, float2 v3) {
+    uint4 h, l;
+    split_pair(v0.x, v0.y, h.x, l.x);
+    split_pair(v1.x, v1.y, h.y, l.y);
+    split_pair(v2.x, v2.y, h.z, l.z);
+    split_pair(v3.x, v3.y, h.w, l.w);
+    const uint32_t off = tc::kmajor_off(row, 2 * x0, K);
+    *(uint4 *)(ah + off) = h;
+    *(uint4 *)(al + off) = l;
 }
 
 // MMAs of one tile: D = A * B^T over K, split-BF16 (hi hi + hi lo + lo hi)
@@ -222,11 +235,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             pt ^= 1u;
             ok = __syncthreads_and(got ? 1 : 0) != 0;
             if (!ok) break;
-#pragma unroll 8
-            for (int xq = 0; xq < DH2; ++xq) {
+#pragma unroll 2
+            for (int xq = 0; xq < DH2; xq += 4) {
                 const int x = half * DH2 + xq;
-                const float2 v = stage[x * kTcRows + row];
-                put_split(ah, al, row, x, K, v.x, v.y);
+                put_split4(ah, al, row, x, K, stage[x * kTcRows + row], stage[(x + 1) * kTcRows + row],
+                           stage[(x + 2) * kTcRows + row], stage[(x + 3) * kTcRows + row]);
             }
         } else {
             if (pending >= 0) {   // the group sum needs the last channel's read-back
@@ -235,10 +248,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             // inverse DFT of the group sum: conj(DFT(conj u))
 #pragma unroll
-            for (int kq = 0; kq < DH2; ++kq) {
-                put_split(ah, al, row, half * DH2 + kq, K, ur[kq], -ui[kq]);
-                ur[kq] = ui[kq] = 0.f;
+            for (int kq = 0; kq < DH2; kq += 4) {
+                put_split4(ah, al, row, half * DH2 + kq, K, make_float2(ur[kq], -ui[kq]),
+                           make_float2(ur[kq + 1], -ui[kq + 1]), make_float2(ur[kq + 2], -ui[kq + 2]),
+                           make_float2(ur[kq + 3], -ui[kq + 3]));
             }
+#pragma unroll
+            for (int kq = 0; kq < DH2; ++kq) ur[kq] = ui[kq] = 0.f;
         }
         tc::fence_smem_async();
         __syncthreads();
