@@ -218,3 +218,19 @@ def test_distinct_lattice_rows_expand_back():
         off += c
         ioff += len(s)
     assert counts[0] < len(sets[0])              # the clustered set repeats angles
+
+
+def test_pack_bytes_round_trip():
+    """The packed device-to-host read-back: mixed dtypes and shapes (odd byte
+    counts padded to 8) come back equal."""
+    import torch
+    from vesper_python_gb300 import align
+    ts = [torch.arange(5, dtype=torch.float32), torch.arange(3, dtype=torch.int32),
+          torch.arange(6, dtype=torch.int64).reshape(2, 3), torch.ones((2, 2, 2), dtype=torch.float64),
+          torch.arange(7, dtype=torch.int16), torch.zeros(0, dtype=torch.float32)]
+    packed, layout = align.pack_bytes(ts)
+    assert packed.dtype == torch.uint8 and all(off % 8 == 0 for off, _, _ in layout)
+    back = align.unpack_bytes(packed.numpy(), layout)
+    for t, a in zip(ts, back):
+        assert a.shape == tuple(t.shape) and np.array_equal(a, t.numpy())
+    assert align.pack_bytes([]) == (None, [])

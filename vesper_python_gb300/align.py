@@ -82,6 +82,32 @@ _NP_DTYPES = {torch.float32: np.dtype(np.float32), torch.float64: np.dtype(np.fl
               torch.uint8: np.dtype(np.uint8)}
 
 
+def pack_bytes(tensors):
+    """The bytes of ``tensors`` (any dtypes in _NP_DTYPES) in one uint8 tensor
+    on their device, each piece starting 8-byte aligned, and the layout
+    [(offset, dtype, shape)] that unpack_bytes reads back; (None, []) for no
+    tensors."""
+    pieces, layout, off = [], [], 0
+    for t in tensors:
+        b = t.contiguous().reshape(-1).view(torch.uint8)
+        pad = (-b.numel()) % 8
+        pieces.append(b)
+        if pad:
+            pieces.append(torch.empty(pad, dtype=torch.uint8, device=b.device))   # filler, never read
+        layout.append((off, _NP_DTYPES[t.dtype], tuple(t.shape)))
+        off += b.numel() + pad
+    return (torch.cat(pieces) if pieces else None), layout
+
+
+def unpack_bytes(buf, layout):
+    """numpy copies of the tensors packed by pack_bytes, from its bytes ``buf``."""
+    out = []
+    for off, dt, shape in layout:
+        n = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
+        out.append(buf[off:off + n].view(dt).reshape(shape).copy())
+    return out
+
+
 def distinct_lattice_rows(key, lens):
     """Distinct lattice rows of consecutive angle lists (list i has lens[i]
     entries; key = their lattice rows, concatenated): the distinct rows pair by
@@ -503,36 +529,17 @@ class Aligner:
         wait: the tensors' bytes are packed on the device (8-byte aligned
         pieces), copied to pinned memory in one transfer, and split on the
         host."""
-        flat = [t.contiguous().reshape(-1) for g in groups for t in g]
-        if not flat:
+        packed, layout = pack_bytes([t for g in groups for t in g])
+        if packed is None:
             return [[] for _ in groups]
-        pieces, offs, off = [], [], 0
-        for t in flat:
-            b = t.view(torch.uint8)
-            pad = (-b.numel()) % 8
-            pieces.append(b)
-            if pad:
-                pieces.append(torch.empty(pad, dtype=torch.uint8, device=b.device))   # filler, never read
-            offs.append(off)
-            off += b.numel() + pad
-        packed = torch.cat(pieces)
         host = getattr(self, "_pinned", None)
         if host is None or host.numel() < packed.numel():   # one pinned buffer, grown on demand
             host = self._pinned = torch.empty(max(packed.numel(), 1 << 20), dtype=torch.uint8, pin_memory=True)
         host[:packed.numel()].copy_(packed, non_blocking=True)
         torch.cuda.current_stream(self.dev.device).synchronize()
-        buf = host.numpy()
-        it = iter(zip(flat, offs))
-        res = []
-        for g in groups:
-            row = []
-            for t in g:
-                ft, o = next(it)
-                dt = _NP_DTYPES[ft.dtype]
-                row.append(buf[o:o + ft.numel() * dt.itemsize].view(dt).reshape(tuple(t.shape)).copy())
-            res.append(row)
+        arrays = iter(unpack_bytes(host.numpy(), layout))
         self.d2h_bytes += packed.numel()
-        return res
+        return [[next(arrays) for _ in g] for g in groups]
 
     def _proposal_subsets(self, p, P, mats):
         """Network scores of every rotation and the exact-search subset
