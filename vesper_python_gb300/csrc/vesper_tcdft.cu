@@ -17,16 +17,22 @@
 // Split-BF16: a float32 value v is held as hi = bf16(v), lo = bf16(v - hi);
 // each product is hi_a hi_b + hi_a lo_b + lo_a hi_b (three MMAs into one
 // float32 accumulator; lo_a lo_b, about 2^-16 of the product, is dropped).
-// The operands keep about 16 significant bits, so results carry relative errors
-// near 1e-5 of the line's magnitude, against near 1e-7 for the float32 FFT.
+// The operands keep about 16 significant bits, so a transform carries relative
+// errors near 1e-5 of the line's magnitude, against near 1e-7 for the float32
+// FFT.
 //
 // One CTA = one M tile of 128 rows, 256 threads: threads t and t + 128 own row
-// t (TMEM lane t), each half of its elements.  Per channel: a TMA box brings
-// the S lines to shared memory, the CTA writes the split tile, one thread issues
-// the 3 * K / 16 MMAs and commits them to an mbarrier, every thread reads its
-// row back with tcgen05.ld and accumulates the product in registers.  Waits
-// are bounded (200 ms of global time); a time-out sets *err, and the CTA waits
-// once more, frees its TMEM and returns.
+// t (TMEM lane t), each half of its elements.  A CTA runs its tiles (the
+// channels of each group, then the group's inverse) as a pipeline: a TMA box
+// brings a channel's S lines to shared memory, the CTA writes the split
+// operand, one thread issues the 3 * K / 16 MMAs into one of two TMEM
+// accumulators and commits them to an mbarrier, and while they run every
+// thread reads back the previous tile (tcgen05.ld) and multiplies it by the
+// target spectrum into the group sum in registers, and the next box loads.
+// The results carry the split-BF16 error described above: measured against a
+// float64 oracle, a few 1e-6 of the largest correlation score.  Waits are
+// bounded (200 ms of global time); a time-out sets *err, and the CTA waits once
+// more, frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
