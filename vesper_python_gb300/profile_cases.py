@@ -6,6 +6,9 @@
   python -m vesper_python_gb300.profile_cases prop
       three learned-proposal scorings (committed weights) of one held-out
       128^3 / 64^3 pair at s = 3 over the 10-degree grid
+  python -m vesper_python_gb300.profile_cases cufft<d> [nrot]
+      comparison only: the FFT work of a mode-V search through cuFFT
+      (torch.fft, no gather) next to this library's whole search, per rotation
   python -m vesper_python_gb300.profile_cases tcb<d>
       the split-BF16 tensor-core pass B alone on random side-d spectra
       (prob layout, 16 rotations), timed
@@ -90,6 +93,50 @@ def main(argv=None):
                 passes = " / ".join(f"{1000 * t / n:.3f}" for t in prof["pass_ms"][:3])
                 print(f"prob side {d} path {path} {label}: {ms:.2f} ms for {n} rotations, "
                       f"{1000 * ms / n:.3f} us per rotation (passes A / B / C {passes} us)")
+    elif what.startswith("cufft"):
+        # comparison only: the FFT work of a mode-V search done by cuFFT
+        # (torch.fft), in batches of 64 rotations of already rotated fields (no
+        # gather): 3 forward real transforms, product with the conjugate target
+        # spectra, channel sum, inverse transform, argmax; next to this
+        # library's whole search (gather included) on the same side
+        d = int(what[5:])
+        nrot = int(argv[1]) if len(argv) > 1 else 1024
+        B = 64
+        g = torch.Generator(device=dev.device).manual_seed(d)
+        x = torch.randn((B, 3, d, d, d), device=dev.device, generator=g)
+        T = torch.fft.rfftn(torch.randn((3, d, d, d), device=dev.device, generator=g), dim=(-3, -2, -1)).conj()
+
+        def cufft_search():
+            for _ in range(0, nrot, B):
+                X = torch.fft.rfftn(x, dim=(-3, -2, -1))
+                r = torch.fft.irfftn((X * T).sum(dim=1), s=(d, d, d), dim=(-3, -2, -1))
+                r.reshape(B, -1).argmax(dim=1)
+
+        rng = np.random.default_rng(d)
+        data = rng.uniform(0.1, 2, size=(d, d, d))
+        data[rng.random((d, d, d)) < 0.5] = 0
+        vec = rng.normal(size=(d, d, d, 3))
+        vec /= np.linalg.norm(vec, axis=-1, keepdims=True)
+        vec[data == 0] = 0
+        td, tv = dev.to_dev(data), dev.to_dev(vec.astype(np.float32))
+        spec = vg.target_spectra_device(td, tv, "VecProduct", 0.0, dev=dev)
+        ang = vg.calc_angle_comb(10.0)[:nrot]
+        mats = dev.to_dev(vg.rot_matrices(ang))
+
+        def ours():
+            vg.search_device(spec, td, tv, "VecProduct", 0.0, mats, dev=dev, tuned=True)
+
+        for name, fn, n in (("cuFFT (torch.fft), no gather", cufft_search, (nrot + B - 1) // B * B),
+                            ("this library's search", ours, len(ang))):
+            fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(3):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            print(f"side {d} {name}: {1000 * e0.elapsed_time(e1) / 3 / n:.3f} us per rotation")
     elif what.startswith("tcb"):
         # the tensor-core pass B alone (vesper_tc_pass_b) on random spectra of
         # side d, prob-mode layout (7 channels, 2 groups), 16 rotations, 3 calls
