@@ -158,3 +158,47 @@ def test_interpolate_oracle_matches_golden(golden_dir):
         a = g[f"in{n}"].copy()
         orc.interpolate(a)
         np.testing.assert_array_equal(a, g[f"out{n}"])
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_get_score_matches_reference_prints(golden_dir, mode):
+    """The oracle's get_score (the checker of the GPU rescoring) against the
+    reference's own printed get_score lines of every refined model of the
+    128^3/64^3 seed-0 pair (search_pair128_<mode>.txt, recorded by
+    make_golden.py from the reference's search_map_fft): Overlap, Nm/total,
+    CC, PCC and Score."""
+    import re
+    g = _g(golden_dir, "search_pair128.npz")
+    txt = open(f"{golden_dir}/search_pair128_{mode}.txt").read()
+    printed = re.findall(r"Overlap=(\S+) (\d+)/(\d+) CC=(\S+) PCC=(\S+)\nScore= (\S+)", txt)
+    angles, trans = g[f"{mode}_refined_angle"], g[f"{mode}_refined_trans"]
+    assert len(printed) == len(angles) > 0
+    st1 = g["stats1"]
+    for k in range(len(angles)):
+        vec, data = orc.rot_mrc(g["data2"], g["vec2"], angles[k])
+        ov, nm, total, cc, pcc, score, _ = orc.get_score(g["data1"], g["vec1"], st1[2], st1[3], st1[4], data, vec,
+                                                         trans[k])
+        p_ov, p_nm, p_total, p_cc, p_pcc, p_score = printed[k]
+        assert (nm, total) == (int(p_nm), int(p_total))
+        assert ov == float(p_ov)
+        for got, want in ((cc, p_cc), (pcc, p_pcc), (score, p_score)):
+            assert abs(got - float(want)) <= 1e-12 * max(1.0, abs(float(want))), (k, got, want)
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_refined_model_translations_match_reference_prints(golden_dir, mode):
+    """convert_trans with euler2rot (the oracle's restatement of :1549-1566)
+    reproduces the reference's printed translation of every refined model,
+    to the printed three decimals."""
+    import re
+    g = _g(golden_dir, "search_pair128.npz")
+    txt = open(f"{golden_dir}/search_pair128_{mode}.txt").read()
+    printed = re.findall(r"\n#(\d+) Rotation= \((\S+) (\S+) (\S+)\) Translation= \((\S+) (\S+) (\S+)\)", txt)
+    angles, trans = g[f"{mode}_refined_angle"], g[f"{mode}_refined_trans"]
+    assert len(printed) == len(angles) > 0
+    d = int(g["dim"])
+    for k, row in enumerate(printed):
+        assert int(row[0]) == k
+        assert np.allclose([float(v) for v in row[1:4]], angles[k])
+        t = orc.convert_trans(g["cent1"], g["cent2"], orc.euler2rot(angles[k]), trans[k], 7.0, d)
+        assert ["{:.3f}".format(v) for v in t] == list(row[4:7]), (k, t, row)
