@@ -202,3 +202,22 @@ def test_refined_model_translations_match_reference_prints(golden_dir, mode):
         assert np.allclose([float(v) for v in row[1:4]], angles[k])
         t = orc.convert_trans(g["cent1"], g["cent2"], orc.euler2rot(angles[k]), trans[k], 7.0, d)
         assert ["{:.3f}".format(v) for v in t] == list(row[4:7]), (k, t, row)
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_global_top_n_matches_reference_prints(golden_dir, mode):
+    """The oracle's stable top-N (score descending, ties to the lower index,
+    :664) over the reference's recorded per-rotation scores of the 30-degree
+    grid gives the rotations the reference printed as M0..M9, in order."""
+    import re
+    g = _g(golden_dir, "search_pair128.npz")
+    txt = open(f"{golden_dir}/search_pair128_{mode}.txt").read()
+    printed = re.findall(r"\nM(\d+) Rotation= \((\S+) (\S+) (\S+)\)", txt)
+    grid = orc.calc_angle_comb(30.0)
+    angles, scores = g[f"{mode}_angles"], g[f"{mode}_score"]
+    assert np.array_equal(angles[:len(grid)], np.asarray(grid, np.float64))   # the grid comes first, in order
+    top = orc.topn(scores[:len(grid)], len(printed))
+    assert len(printed) == 10
+    for k, (i, a, b, c) in enumerate(printed):
+        assert int(i) == k
+        assert np.allclose(grid[top[k]], [float(a), float(b), float(c)]), (k, grid[top[k]], (a, b, c))
