@@ -349,6 +349,12 @@ int vesper_topk_subset_batch(const float *scores, int nbatch, int n, int k, int3
  * :880-962) when the search option selects it. */
 int vesper_tc_pass_b(const void *S, const void *T, void *U, int d, int nch, int ngrp, int split, int nbatch, int *err,
                      void *stream);
+/* Failure self-test of the same kernel (one rotation): every CTA first waits
+ * on a barrier that nothing completes, gives up after limit_ms (1..1000),
+ * sets *err = 1, frees its TMEM and returns without touching U.  The context
+ * stays usable.  No counterpart in the reference. */
+int vesper_tc_pass_b_stall_test(const void *S, const void *T, void *U, int d, int nch, int ngrp, int split,
+                                int limit_ms, int *err, void *stream);
 
 #ifdef __cplusplus
 }

@@ -124,3 +124,48 @@ def test_vec_search_tensor_pass_b_side32(dev):
     diff = la.cpu().numpy()[:, 0] != lb.cpu().numpy()[:, 0]
     assert np.all(np.abs(sa - sb)[diff] < 5e-4 * scale)
     assert int(diff.sum()) <= max(1, len(sa) // 50)
+
+
+def test_tc_wait_timeout_is_reported_and_context_survives(dev):
+    """Failure detection without a fault: the stall self-test makes every CTA
+    wait on a barrier that nothing completes; the bounded wait gives up after
+    20 ms, the status word reads 1, and the same context then runs the pass
+    correctly."""
+    from vesper_python_gb300 import _native
+    d, nch, ngrp, split = 32, 7, 2, 3
+    rng = np.random.default_rng(9)
+    H = d // 2 + 1
+    S = rng.normal(size=(1, nch, d, d, H)) + 1j * rng.normal(size=(1, nch, d, d, H))
+    T = rng.normal(size=(nch, d, d, H)) + 1j * rng.normal(size=(nch, d, d, H))
+    St, Tt = dev.to_dev(S.astype(np.complex64)), dev.to_dev(T.astype(np.complex64))
+    U = torch.zeros((1, ngrp) + S.shape[2:], dtype=torch.complex64, device=dev.device)
+    err = torch.zeros(1, dtype=torch.int32, device=dev.device)
+    _native.check(dev.lib.vesper_tc_pass_b_stall_test(ctypes.c_void_p(St.data_ptr()), ctypes.c_void_p(Tt.data_ptr()),
+                                                      ctypes.c_void_p(U.data_ptr()), d, nch, ngrp, split, 20,
+                                                      ctypes.c_void_p(err.data_ptr()), dev.stream))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 1
+    assert float(U.abs().max().item()) == 0.0        # nothing written
+    got, err2 = _run(dev, S, T, ngrp, split)
+    assert err2 == 0
+    want = _want(S, T, ngrp, split)
+    assert np.max(np.abs(got - want)) / np.max(np.abs(want)) < 1e-4
+
+
+def test_search_is_deterministic(dev):
+    """The same search twice gives the same bits (float32 path and the
+    tensor-core path): the argmax keys are atomic maxima and every reduction
+    has a fixed order."""
+    from oracle import vesper_oracle as orc
+    from vesper_python_gb300 import vesper as vg
+    d = 32
+    rng = np.random.default_rng(21)
+    tdata, tvec, _ = _fields(rng, d, 0.5)
+    qdata, qvec, _ = _fields(rng, d, 0.5)
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), "VecProduct", 0.0, dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(orc.calc_angle_comb(30.0)[::5]))
+    qd, qv = dev.to_dev(qdata), dev.to_dev(qvec)
+    for path in (-1, 3):
+        a = vg.search_device(spec, qd, qv, "VecProduct", 0.0, mats, dev=dev, opts=(path, 0, 0))
+        b = vg.search_device(spec, qd, qv, "VecProduct", 0.0, mats, dev=dev, opts=(path, 0, 0))
+        assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1]), path

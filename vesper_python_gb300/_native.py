@@ -145,6 +145,7 @@ SIGNATURES = {
     "vesper_topk_subset": [_vp, _i, _i, _vp, _vp],
     "vesper_topk_subset_batch": [_vp, _i, _i, _i, _vp, _vp],
     "vesper_tc_pass_b": [_vp, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp],
+    "vesper_tc_pass_b_stall_test": [_vp, _vp, _vp, _i, _i, _i, _i, _i, _vp, _vp],
     "vesper_search_status": [_vp, _sz, _vp, _vp],
 }
 

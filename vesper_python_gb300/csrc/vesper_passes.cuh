@@ -163,7 +163,8 @@ struct PassB2 {
 // pass B on the tensor cores (split-BF16 DFTs; vesper_tcdft.cu), sides 32 and 64
 bool tc_pass_b_supported(int d);
 int tc_pass_b_wave(int d);   // rotations per full wave of its CTAs
-int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st);
+int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st, int stall = 0,
+              uint64_t limit_ns = 200ull * 1000000);
 
 __host__ __device__ inline size_t smem_b2(int d, int ntab, int nch, int ngrp, int W) {
     return smem_head(d, ntab) + (size_t)(nch + ngrp) * d * W * sizeof(float2);

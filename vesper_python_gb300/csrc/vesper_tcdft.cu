@@ -31,8 +31,9 @@
 // target spectrum into the group sum in registers, and the next box loads.
 // The results carry the split-BF16 error described above: measured against a
 // float64 oracle, a few 1e-6 of the largest correlation score.  Waits are
-// bounded (200 ms of global time); a time-out sets *err, and the CTA waits once
-// more, frees its TMEM and returns.
+// bounded (200 ms of global time unless the caller gives a limit); a time-out
+// sets *err, and the CTA waits once more, frees its TMEM and returns
+// (vesper_tc_pass_b_stall_test runs that path on purpose).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -50,7 +51,6 @@ namespace vg {
 
 constexpr int kTcRows = 128;                     // M: columns j per CTA
 constexpr int kTcThreads = 256;                  // two threads per row: each takes half of its elements
-constexpr uint64_t kTcWaitNs = 200ull * 1000000; // bound on one mbarrier wait
 
 template <int D>
 struct TcGeom {
@@ -137,7 +137,8 @@ __device__ __forceinline__ void issue_split_mma(uint32_t tmem, const unsigned ch
 
 template <int D>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_tcb(const PassB2 a, const unsigned char *tab, const __grid_constant__ CUtensorMap tmS, int *err) {
+    k_tcb(const PassB2 a, const unsigned char *tab, const __grid_constant__ CUtensorMap tmS, int *err, int stall,
+          uint64_t limit_ns) {
     using G = TcGeom<D>;
     constexpr int K = G::K;
     constexpr int H = D / 2 + 1;
@@ -174,6 +175,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);   // this warp's 32 lanes
     uint32_t pm = 0, pt = 0;   // phases of the MMA and TMA barriers
     bool ok = true;
+    if (stall) {   // failure self-test: a wait that nothing completes (no copy was issued)
+        const bool got = tc::mbar_wait(mbar_tma, pt, limit_ns);
+        pt ^= 1u;
+        ok = __syncthreads_and(got ? 1 : 0) != 0;
+    }
 
     // Tiles of one CTA, in order: the channels of group 0, its inverse, then
     // (two groups) the channels of group 1 and its inverse.  Tile t's MMAs
@@ -233,11 +239,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tc::fence_before_sync();
     };
 
-    if (tid == 0) load_s(0);
+    if (tid == 0 && ok) load_s(0);
     int pending = -1;   // tile whose read-back is still to do
     for (int t = 0; t < ntiles && ok; ++t) {
         if (!is_inv(t)) {
-            const bool got = tc::mbar_wait(mbar_tma, pt, kTcWaitNs);
+            const bool got = tc::mbar_wait(mbar_tma, pt, limit_ns);
             pt ^= 1u;
             ok = __syncthreads_and(got ? 1 : 0) != 0;
             if (!ok) break;
@@ -271,7 +277,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         if (pending >= 0) epilogue(pending);   // overlaps this tile's MMAs
         pending = t;
-        const bool got = tc::mbar_wait(mbar_mma, pm, kTcWaitNs);
+        const bool got = tc::mbar_wait(mbar_mma, pm, limit_ns);
         pm ^= 1u;
         tc::fence_after_sync();
         ok = __syncthreads_and(got ? 1 : 0) != 0;   // MMAs done: the operand tile is free
@@ -281,8 +287,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (tid == 0) atomicExch(err, 1);
         // work of the timed-out step may still run: wait for both barriers
         // once more (bounded) before the TMEM goes back
-        tc::mbar_wait(mbar_mma, pm ^ 1u, kTcWaitNs);
-        tc::mbar_wait(mbar_tma, pt ^ 1u, kTcWaitNs);
+        tc::mbar_wait(mbar_mma, pm ^ 1u, limit_ns);
+        tc::mbar_wait(mbar_tma, pt ^ 1u, limit_ns);
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -360,7 +366,7 @@ static bool box_map(CUtensorMap *m, const void *base, int D, int dH, int planes)
 
 // pass B of nb rotations on the tensor cores; err: device int, set to 1 when
 // a wait timed out (left untouched otherwise)
-int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st) {
+int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st, int stall, uint64_t limit_ns) {
     if (nb < 1 || nb > 65535 || !err) return fail(VESPER_ERR_INVALID, "tc pass B: bad batch");
     auto run = [&](auto dc) -> int {
         constexpr int D = decltype(dc)::value;
@@ -372,7 +378,8 @@ int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st) {
         CUtensorMap tmS;
         if ((dH * 8) % 16 || !box_map(&tmS, a.S, D, dH, nb * a.nch))
             return fail(VESPER_ERR_CUDA, "tc pass B: tensor map (driver entry point or alignment)");
-        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcThreads, sm, st>>>(a, tab, tmS, err);
+        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcThreads, sm, st>>>(a, tab, tmS, err, stall,
+                                                                                 limit_ns);
         VG_CHECK_LAUNCH("k_tcb");
         return VESPER_OK;
     };
@@ -384,6 +391,23 @@ int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st) {
 }  // namespace vg
 
 using namespace vg;
+
+extern "C" int vesper_tc_pass_b_stall_test(const void *S, const void *T, void *U, int d, int nch, int ngrp,
+                                           int split, int limit_ms, int *err, void *stream) {
+    if (!S || !T || !U || !err || nch < 1 || ngrp < 1 || ngrp > 2 || split < 1 || split > nch || limit_ms < 1 ||
+        limit_ms > 1000)
+        return fail(VESPER_ERR_INVALID, "vesper_tc_pass_b_stall_test: bad args");
+    if (ngrp == 2 && split >= nch) return fail(VESPER_ERR_INVALID, "vesper_tc_pass_b_stall_test: empty second group");
+    PassB2 a{};
+    a.S = (const float2 *)S;
+    a.T = (const float2 *)T;
+    a.U = (float2 *)U;
+    a.d = d;
+    a.nch = nch;
+    a.ngrp = ngrp;
+    a.split = ngrp == 1 ? nch : split;
+    return tc_pass_b(a, 1, err, (cudaStream_t)stream, 1, (uint64_t)limit_ms * 1000000ull);
+}
 
 extern "C" int vesper_tc_pass_b(const void *S, const void *T, void *U, int d, int nch, int ngrp, int split,
                                 int nbatch, int *err, void *stream) {
