@@ -221,3 +221,18 @@ def test_global_top_n_matches_reference_prints(golden_dir, mode):
     for k, (i, a, b, c) in enumerate(printed):
         assert int(i) == k
         assert np.allclose(grid[top[k]], [float(a), float(b), float(c)]), (k, grid[top[k]], (a, b, c))
+
+
+def test_prob_refined_models_match_reference(golden_dir):
+    """The oracle's mixed pass (with the statistics of its own first pass)
+    over the reference's refined prob-mode models: mixed score times 1/d^3,
+    and the mixed and vector translations of every model."""
+    g = _g(golden_dir, "prob_pair128.npz")
+    d = int(g["dim"])
+    rd3 = 1.0 / d ** 3
+    tspec = orc.target_spectra([g["vec1"][..., 0], g["vec1"][..., 1], g["vec1"][..., 2]] + list(g["probs1"]))
+    st = orc.prob_stats(g["pass1_vscore"], g["pass1_pscore"], rd3)
+    for k, a in enumerate(g["refined_angle"]):
+        res = orc.rot_and_search_prob(tspec, g["data2"], g["vec2"], g["probs2"], a, 0.5, st, promotion="numpy2")
+        assert abs(np.float64(res[4]) * rd3 - g["refined_mixed"][k]) <= 1e-15 * abs(g["refined_mixed"][k])
+        assert tuple(res[5]) == tuple(g["refined_mtrans"][k]) and tuple(res[1]) == tuple(g["refined_vtrans"][k])
