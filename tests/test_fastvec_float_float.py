@@ -9,11 +9,10 @@ float64, which holds a 24 x 24-bit product exactly) plus the cross terms with
 fmaf; sums: TwoSum, the low parts, then FastTwoSum.  The same operation order
 as the kernels.
 """
-import io
 import contextlib
+import io
 
 import numpy as np
-import pytest
 
 from oracle import vesper_oracle as orc
 
