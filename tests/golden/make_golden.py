@@ -17,6 +17,9 @@ Outputs (committed):
   search_pair128_*.txt  the reference's stdout for each mode
   prob_pair128.npz    prob-mode per-rotation results, statistics and top-N
   prob_pair128.txt    the reference's stdout
+  voxsize_cases.npz   mrc_set_vox_size on small maps (thresholds incl. the
+                      negative-shift path, two voxel sizes): digests of data
+                      and dens, the new grid and the printed lines
 
 The coarse fields feeding the search goldens come from the C restatement of
 doFastVEC (the pure-Python reference loop is far too slow at 65^3 windows);
@@ -280,8 +283,37 @@ def gen_prob_pair():
         f.write(setup + buf.getvalue())
 
 
+def gen_voxsize():
+    """mrc_set_vox_size (VESPER_1_prob_new.py:59-118) on small random maps with
+    negative values: thresholds 0, 0.25 and -0.3 (the shift path), voxel
+    sizes 2 and 5, non-cubic maps and non-zero origins; the thresholded data,
+    dens, the new grid (xdim, orig, cent) and the printed lines."""
+    rng = np.random.default_rng(77)
+    out = {}
+    k = 0
+    for si, (shape, orig, width) in enumerate((((24, 28, 20), (1.5, -2.0, 0.25), 1.0),
+                                               ((31, 31, 31), (0.0, 0.0, 0.0), 1.5))):
+        base = (rng.normal(size=shape) * 0.4).astype(np.float32)
+        out[f"src{si}"] = base
+        for th in (0.0, 0.25, -0.3):
+            for vs in (2.0, 5.0):
+                m = refshim.make_mrc_obj(ref, base, width, orig)
+                buf = io.StringIO()
+                with contextlib.redirect_stdout(buf):
+                    m, n = ref.mrc_set_vox_size(m, th, vs)
+                out[f"c{k}_params"] = np.array([si, width, *orig, th, vs], np.float64)
+                # thresholded data and dens as digests of their bytes (float32 / float64)
+                out[f"c{k}_digest"] = np.array([digest(np.asarray(m.data, np.float32)),
+                                                digest(np.asarray(m.dens, np.float64).reshape(-1))])
+                out[f"c{k}_grid"] = np.array([n.xdim, *n.orig, *n.cent], np.float64)
+                out[f"c{k}_print"] = np.array(buf.getvalue())
+                k += 1
+    out["ncase"] = np.array(k)
+    np.savez_compressed(os.path.join(HERE, "voxsize_cases.npz"), **out)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["angles", "rot", "fastvec", "search", "prob"]
+    which = sys.argv[1:] or ["angles", "rot", "fastvec", "search", "prob", "voxsize"]
     if "angles" in which:
         gen_angles()
     if "rot" in which:
@@ -292,3 +324,5 @@ if __name__ == "__main__":
         gen_search_pair128()
     if "prob" in which:
         gen_prob_pair()
+    if "voxsize" in which:
+        gen_voxsize()
