@@ -56,7 +56,8 @@ def digest(*arrays):
 
 def gen_angles():
     out = {}
-    for a in (30.0, 15.0, 10.0, 45.0, 60.0, 20.0, 90.0):
+    # steps that divide 360 and steps that do not (the grid's range ends)
+    for a in (30.0, 15.0, 10.0, 45.0, 60.0, 20.0, 90.0, 7.0, 25.0, 7.5, 50.0, 100.0):
         out[f"A{a:g}"] = ref.calc_angle_comb(a)
     np.savez_compressed(os.path.join(HERE, "angles.npz"), **out)
 
