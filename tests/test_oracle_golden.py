@@ -236,3 +236,19 @@ def test_prob_refined_models_match_reference(golden_dir):
         res = orc.rot_and_search_prob(tspec, g["data2"], g["vec2"], g["probs2"], a, 0.5, st, promotion="numpy2")
         assert abs(np.float64(res[4]) * rd3 - g["refined_mixed"][k]) <= 1e-15 * abs(g["refined_mixed"][k])
         assert tuple(res[5]) == tuple(g["refined_mtrans"][k]) and tuple(res[1]) == tuple(g["refined_vtrans"][k])
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_refinement_angle_list_matches_reference(golden_dir, mode):
+    """The refinement angles the reference searched (its recorded calls after
+    the 30-degree grid, duplicates included, in order) are refine_angle_list
+    of its top-N, for the oracle's loop and the package's vectorised form."""
+    from vesper_python_gb300 import vesper as vg
+    g = _g(golden_dir, "search_pair128.npz")
+    grid = orc.calc_angle_comb(30.0)
+    angles, scores = g[f"{mode}_angles"], g[f"{mode}_score"]
+    top = orc.topn(scores[:len(grid)], 10)
+    want = angles[len(grid):]
+    tops = [grid[t] for t in top]
+    assert np.array_equal(vg.refine_angle_list(tops), want)
+    assert np.array_equal(np.asarray(orc.refine_angles(tops), np.float64), want)
