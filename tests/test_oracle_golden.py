@@ -252,3 +252,16 @@ def test_refinement_angle_list_matches_reference(golden_dir, mode):
     tops = [grid[t] for t in top]
     assert np.array_equal(vg.refine_angle_list(tops), want)
     assert np.array_equal(np.asarray(orc.refine_angles(tops), np.float64), want)
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_refined_top_n_matches_reference(golden_dir, mode):
+    """The stable top-N over the reference's recorded refinement scores
+    (duplicated angles included: ties go to the first occurrence) is its
+    refined model list, angles and translations in order."""
+    g = _g(golden_dir, "search_pair128.npz")
+    n = len(orc.calc_angle_comb(30.0))
+    angles, scores, trans = g[f"{mode}_angles"][n:], g[f"{mode}_score"][n:], g[f"{mode}_trans"][n:]
+    top = orc.topn(scores, len(g[f"{mode}_refined_angle"]))
+    assert np.array_equal(angles[top], g[f"{mode}_refined_angle"])
+    assert np.array_equal(trans[top], g[f"{mode}_refined_trans"])
