@@ -20,6 +20,7 @@ Outputs (committed):
   voxsize_cases.npz   mrc_set_vox_size on small maps (thresholds incl. the
                       negative-shift path, two voxel sizes): digests of data
                       and dens, the new grid and the printed lines
+  show_vec_cases.npz  show_vec's PDB files (names and text) for two models
 
 The coarse fields feeding the search goldens come from the C restatement of
 doFastVEC (the pure-Python reference loop is far too slow at 65^3 windows);
@@ -313,8 +314,34 @@ def gen_voxsize():
     np.savez_compressed(os.path.join(HERE, "voxsize_cases.npz"), **out)
 
 
+def gen_show_vec():
+    """show_vec (VESPER_1_prob_new.py:1144-1208): the PDB files the reference
+    writes for two small models (translations wrapping past d/2 and negative
+    scores included), stored as text."""
+    import tempfile
+    from pathlib import Path
+    rng = np.random.default_rng(91)
+    out = {}
+    for k, (d, trans, score, rank) in enumerate(((5, (4, 1, 0), 12.3456, 3), (7, (0, 6, 3), -3.25, 11))):
+        data = np.where(rng.random((d, d, d)) < 0.35, rng.uniform(0.5, 2, (d, d, d)), 0.0)
+        vec = rng.normal(size=(d, d, d, 3)).astype(np.float32)
+        sco = rng.normal(size=(d, d, d))
+        origin = rng.uniform(-20, 20, size=3)
+        with tempfile.TemporaryDirectory() as tmp:
+            with contextlib.redirect_stdout(io.StringIO()):
+                ref.show_vec(origin, vec, data, sco, score, 7.0, trans, (0, 0, 0), Path(tmp), rank)
+            names = sorted(os.listdir(tmp))
+            assert len(names) == 1
+            out[f"c{k}_name"] = np.array(names[0])
+            with open(os.path.join(tmp, names[0])) as f:
+                out[f"c{k}_text"] = np.array(f.read())
+        out[f"c{k}_data"], out[f"c{k}_vec"], out[f"c{k}_sco"] = data, vec, sco
+        out[f"c{k}_params"] = np.array([*origin, *trans, score, rank], np.float64)
+    np.savez_compressed(os.path.join(HERE, "show_vec_cases.npz"), **out)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["angles", "rot", "fastvec", "search", "prob", "voxsize"]
+    which = sys.argv[1:] or ["angles", "rot", "fastvec", "search", "prob", "voxsize", "showvec"]
     if "angles" in which:
         gen_angles()
     if "rot" in which:
@@ -327,3 +354,5 @@ if __name__ == "__main__":
         gen_prob_pair()
     if "voxsize" in which:
         gen_voxsize()
+    if "showvec" in which:
+        gen_show_vec()

@@ -261,3 +261,20 @@ def test_set_vox_size_cases_match_reference(golden_dir):
         assert digest(np.asarray(m.data, np.float32)) == str(g[f"c{k}_digest"][0]), k
         assert digest(np.asarray(m.dens, np.float64).reshape(-1)) == str(g[f"c{k}_digest"][1]), k
         assert np.array_equal(np.array([n.xdim, *n.orig, *n.cent], np.float64), g[f"c{k}_grid"]), k
+
+
+def test_show_vec_writes_the_reference_files(golden_dir, tmp_path):
+    """show_vec writes the same file name and the same bytes as the
+    reference's writer (two models: a translation past d/2 and a negative
+    score)."""
+    from vesper_python_gb300 import vesper as vg
+    g = np.load(f"{golden_dir}/show_vec_cases.npz")
+    for k in range(2):
+        p = g[f"c{k}_params"]
+        origin, trans, score, rank = p[0:3], tuple(int(v) for v in p[3:6]), float(p[6]), int(p[7])
+        out = tmp_path / f"case{k}"
+        out.mkdir()
+        vg.show_vec(origin, g[f"c{k}_vec"], g[f"c{k}_data"], g[f"c{k}_sco"], score, 7.0, trans, (0, 0, 0), out, rank)
+        files = sorted(x.name for x in out.iterdir())
+        assert files == [str(g[f"c{k}_name"])]
+        assert (out / files[0]).read_text() == str(g[f"c{k}_text"])
