@@ -21,6 +21,7 @@ Outputs (committed):
                       negative-shift path, two voxel sizes): digests of data
                       and dens, the new grid and the printed lines
   show_vec_cases.npz  show_vec's PDB files (names and text) for two models
+  fastvec_noncubic.npz doFastVEC on non-cubic sources (windows clipped)
 
 The coarse fields feeding the search goldens come from the C restatement of
 doFastVEC (the pure-Python reference loop is far too slow at 65^3 windows);
@@ -138,6 +139,35 @@ def gen_fastvec_small():
         out[f"c{i}_vec"] = res.vec
         out[f"c{i}_stats"] = np.array([res.dsum, res.Nact, res.ave, res.std, res.std_norm_ave], np.float64)
     np.savez_compressed(os.path.join(HERE, "fastvec_small.npz"), **out)
+
+
+def gen_fastvec_noncubic():
+    """doFastVEC (pure-Python reference loop) on non-cubic sources, with the
+    destination grid reaching past the source on some axes (windows clipped at
+    both ends)."""
+    rng = np.random.default_rng(12)
+    out = {}
+    cases = [
+        # (src shape, src width, src orig, dest dim, dest width, dest orig, dreso)
+        ((20, 14, 17), 1.0, (0.0, 1.5, -2.0), 7, 3.0, (-1.0, 0.5, 0.0), 4.0),
+        ((12, 19, 15), 1.25, (3.0, 0.0, 0.0), 6, 3.5, (2.0, -4.0, 1.5), 3.0),
+    ]
+    for i, (shape, sw, so, dd, dw, do, g) in enumerate(cases):
+        src = np.zeros(shape, np.float32)
+        m = synth.make_blob_map(rng, max(shape), 10, min(shape) * 0.35, sigma=1.2).astype(np.float32)
+        src[...] = m[:shape[0], :shape[1], :shape[2]]
+        src[src < 0.1] = 0.0
+        sobj = refshim.make_mrc_obj(ref, src, sw, so)
+        dobj = refshim.make_mrc_obj(ref, np.zeros((dd,) * 3), dw, (0, 0, 0))
+        dobj.orig = np.array(do, np.float64)
+        dobj.xwidth = dw
+        with contextlib.redirect_stdout(io.StringIO()):
+            res = ref.fastVEC(sobj, dobj, dreso=g)
+        out[f"c{i}_src"] = src
+        out[f"c{i}_params"] = np.array([sw, *so, dd, dw, *do, g], np.float64)
+        out[f"c{i}_data"] = res.data
+        out[f"c{i}_vec"] = res.vec
+    np.savez_compressed(os.path.join(HERE, "fastvec_noncubic.npz"), **out)
 
 
 def _patch_fastvec_with_oracle():
@@ -341,7 +371,7 @@ def gen_show_vec():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["angles", "rot", "fastvec", "search", "prob", "voxsize", "showvec"]
+    which = sys.argv[1:] or ["angles", "rot", "fastvec", "search", "prob", "voxsize", "showvec", "noncubic"]
     if "angles" in which:
         gen_angles()
     if "rot" in which:
@@ -356,3 +386,5 @@ if __name__ == "__main__":
         gen_voxsize()
     if "showvec" in which:
         gen_show_vec()
+    if "noncubic" in which:
+        gen_fastvec_noncubic()

@@ -150,3 +150,15 @@ def test_float_float_blob_map():
     with contextlib.redirect_stdout(io.StringIO()):
         _, mn = vg.mrc_set_vox_size(m, 0.1, 3.0)
     _check(m.data, np.float64(m.xwidth), m.orig.astype(f64), mn.xdim, 3.0, mn.orig, 16.0, rel_tol=1e-13)
+
+
+def test_float_float_noncubic_sources(golden_dir):
+    g = np.load(f"{golden_dir}/fastvec_noncubic.npz")
+    for i in range(2):
+        sw, so0, so1, so2, dd, dw, do0, do1, do2, gg = g[f"c{i}_params"]
+        data, vec = fastvec_float_float(g[f"c{i}_src"], sw, np.array([so0, so1, so2], f64), int(dd), dw,
+                                        np.array([do0, do1, do2], f64), gg)
+        rd = g[f"c{i}_data"]
+        assert np.array_equal(data != 0, rd != 0)
+        assert np.max(np.abs(data - rd)[rd != 0] / np.abs(rd[rd != 0])) < 1e-13
+        assert np.max(np.abs(vec - g[f"c{i}_vec"])) < 2e-6

@@ -265,3 +265,17 @@ def test_refined_top_n_matches_reference(golden_dir, mode):
     top = orc.topn(scores, len(g[f"{mode}_refined_angle"]))
     assert np.array_equal(angles[top], g[f"{mode}_refined_angle"])
     assert np.array_equal(trans[top], g[f"{mode}_refined_trans"])
+
+
+def test_fastvec_noncubic_sources(golden_dir):
+    """C restatement of doFastVEC on non-cubic sources whose windows are
+    clipped at both ends, against the reference loop."""
+    g = _g(golden_dir, "fastvec_noncubic.npz")
+    for i in range(2):
+        sw, so0, so1, so2, dd, dw, do0, do1, do2, gg = g[f"c{i}_params"]
+        data, vec = orc.fastvec(g[f"c{i}_src"], sw, np.float32([so0, so1, so2]), int(dd), dw, [do0, do1, do2], gg)
+        rd = g[f"c{i}_data"]
+        assert np.count_nonzero(rd) > 10
+        assert np.array_equal(data != 0, rd != 0)
+        assert np.max(np.abs(data - rd) / np.maximum(np.abs(rd), 1e-300)) < 1e-15
+        assert np.array_equal(vec, g[f"c{i}_vec"])
