@@ -53,6 +53,14 @@ const char *vesper_last_error(void);
 /* Largest grid side ``dim`` the search kernels accept for ``mode``. */
 int vesper_max_dim(int mode);
 
+/* Measurement helper (no counterpart in the reference): launches
+ * blocks x threads threads that each run independent float32 FMA chains for
+ * ``iters`` steps on ``stream``; *flops_out (HOST) receives the launch's
+ * floating-point operations, so events around the call give the device's
+ * FP32 FMA rate.  ``out`` is DEVICE float[blocks] (written only in a case no
+ * input reaches). */
+int vesper_fp32_peak_probe(int blocks, int threads, int iters, float *out, double *flops_out, void *stream);
+
 /* FFT length rule of the grid side: 1 if ``n`` = 2^a 3^b 5^c 7^d 11^e 13^f
  * with e+f <= 1 (pyFFTW next_fast_len, VESPER_1_prob_new.py:97), else 0. */
 int vesper_fast_len_ok(int n);
@@ -207,11 +215,14 @@ int vesper_search_plan(int dim, int mode, int batch, int nrot, const int *opts, 
  * pre-allocated inputs and outputs under a fixed device-memory budget).  Its
  * scratch is a fixed 16 MiB array inside this library, reserved on every GPU
  * that loads the library until the process exits; it allocates nothing.
- * Same arguments and results as vesper_search with batch = 1.  Rejects, with
+ * Same arguments and results as vesper_search, run with the largest
+ * pipeline batch whose scratch fits the array.  Rejects, with
  * VESPER_ERR_UNSUPPORTED, any call whose
  * vesper_search_workspace_size(dim, mode, 1, nrot) exceeds 16 MiB (mode V
  * fits up to dim 75 with the 24,624 rotations of a 10-degree grid).  The
- * first call on each device looks up the array's device address: make it
+ * first call on each device looks up the array's device address, and the
+ * first call for each (mode, dim) loads that side's kernels and sets their
+ * shared-memory limits: make one call for every (mode, dim) you will use
  * before any stream capture.  All calls share the array, so calls that
  * overlap on the GPU (other streams or host threads) race: serialise them. */
 int vesper_search_static(const void *spectra, const double *data, const float *vec, const float *probs, int dim,

@@ -514,8 +514,18 @@ extern "C" int vesper_search_static(const void *spectra, const double *data, con
         return fail(VESPER_ERR_UNSUPPORTED,
                     "vesper_search_static: dim=%d mode=%d nrot=%d needs %zu bytes of scratch, above its fixed %zu "
                     "(use vesper_search with a workspace)", dim, mode, nrot, need, (size_t)kStaticScratchBytes);
-    // one rotation per pipeline step; the keys each rotation reads are zeroed by
-    // its own first pass, so nothing left in the array by an earlier call matters
-    return search_impl(spectra, data, vec, probs, dim, mode, ave, rotmats, nrot, mix, scores_out, lin_out, 1, scratch,
-                       kStaticScratchBytes, stream, nullptr);
+    // the largest pipeline batch (up to the library default) whose scratch fits
+    // the array; every batch gives the same results, larger ones fewer launches
+    int batch = 1;
+    for (int b = default_batch(dim, mode); b > 1; b = b * 3 / 4) {
+        size_t nb = 0;
+        if (vesper_search_workspace_size(dim, mode, b, nrot, &nb) == VESPER_OK && nb <= kStaticScratchBytes) {
+            batch = b;
+            break;
+        }
+    }
+    // the keys each rotation reads are zeroed by its own first pass, so nothing
+    // left in the array by an earlier call matters
+    return search_impl(spectra, data, vec, probs, dim, mode, ave, rotmats, nrot, mix, scores_out, lin_out, batch,
+                       scratch, kStaticScratchBytes, stream, nullptr);
 }
