@@ -1,21 +1,22 @@
-"""Small, self-contained cases for profiler captures of single kernels.
+"""Small, self-contained cases for profiler captures of single kernels, run
+through ``python bench.py --case <name> [arg]``:
 
-  python -m vesper_python_gb300.profile_cases search<d> [nrot]
+  search<d> [nrot]
       three register/fused-path searches of seeded random side-d fields over
       the first nrot (default 1008) rotations of the 30-degree grid
-  python -m vesper_python_gb300.profile_cases prop
+  prop
       three learned-proposal scorings (committed weights) of one held-out
       128^3 / 64^3 pair at s = 3 over the 10-degree grid
-  python -m vesper_python_gb300.profile_cases cufft<d> [nrot]
+  cufft<d> [nrot]
       comparison only: the FFT work of a mode-V search through cuFFT
       (torch.fft, no gather) next to this library's whole search, per rotation
-  python -m vesper_python_gb300.profile_cases tcb<d>
+  tcb<d>
       the split-BF16 tensor-core pass B alone on random side-d spectra
       (prob layout, 16 rotations), timed
-  python -m vesper_python_gb300.profile_cases fastvec
+  fastvec
       fastVEC of both maps of the seed-0 128^3 / 64^3 generator pair at s = 3,
       g = 16 (the learned-proposal workload's maps), timed per map
-  python -m vesper_python_gb300.profile_cases prob<d>
+  prob<d>
       prob-mode searches (both passes) of seeded random side-d fields with
       four probability channels over the 15-degree grid, timed per kernel
       family (at sides 32 and 64 also with pass B on the tensor cores)
@@ -30,8 +31,8 @@ import sys
 import numpy as np
 import torch
 
-from . import proposal as P
-from . import vesper as vg
+from vesper_python_gb300 import proposal as P
+from vesper_python_gb300 import vesper as vg
 
 
 def main(argv=None):
@@ -142,7 +143,7 @@ def main(argv=None):
         # side d, prob-mode layout (7 channels, 2 groups), 16 rotations, 3 calls
         import ctypes
 
-        from . import _native
+        from vesper_python_gb300 import _native
         d = int(what[3:])
         H = d // 2 + 1
         nb = 16
@@ -166,7 +167,7 @@ def main(argv=None):
         import contextlib
         import io
 
-        from . import synth
+        from vesper_python_gb300 import synth
         pair = synth.workload_pair("prop128_s3_a10", seed=0)
         for name, (src, orig) in (("map1", (pair.map1, pair.orig1)), ("map2", (pair.map2, pair.orig2))):
             m = vg.mrc_obj.from_array(src, 1.0, orig)
@@ -196,5 +197,3 @@ def main(argv=None):
     print("ok", what)
 
 
-if __name__ == "__main__":
-    main()

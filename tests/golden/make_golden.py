@@ -3,7 +3,7 @@ reference module (imported under stand-in modules, see refshim.py).
 
 Run in a container that has the reference checkout:
 
-    VESPER_REFERENCE_DIR=/root/reference python tests/golden/make_golden.py
+    VESPER_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 
 Outputs (committed):
   angles.npz          calc_angle_comb for several steps

@@ -2,7 +2,7 @@
 interpolation_functions.py:6-135): the UNMODIFIED reference function run
 under the stand-in modules of refshim.py on small seeded arrays.
 
-    VESPER_REFERENCE_DIR=/root/reference python tests/golden/make_golden_interp.py
+    VESPER_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden_interp.py
 
 Under the identity jit the reference's mean accumulates in float32 (numpy
 scalars), where numba accumulates in float64; the inputs are multiples of

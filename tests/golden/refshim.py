@@ -103,7 +103,9 @@ def _install_standins():
 
 
 def import_reference(ref_dir: str | None = None):
-    ref_dir = ref_dir or os.environ.get("VESPER_REFERENCE_DIR", "/root/reference")
+    ref_dir = ref_dir or os.environ.get("VESPER_REFERENCE_DIR")
+    if not ref_dir:
+        raise RuntimeError("set VESPER_REFERENCE_DIR to a checkout of the reference (VESPER_Python)")
     _install_standins()
     if ref_dir not in sys.path:
         sys.path.insert(0, ref_dir)
