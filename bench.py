@@ -5,7 +5,7 @@ grid sizing, fastVEC of both maps, target spectra, the rotational search,
 top-N, the +-5 degree refinement, the rotated top-N models and their float64
 scores), on seeded synthetic maps.
 
-Default workload ``prop128_s3_a10``: 128^3 / 64^3 blob-map pairs (the
+Headline workload ``prop128_s3_a10``: 128^3 / 64^3 blob-map pairs (the
 128^3/64^3 generator) at s = 3, A = 10 (24624 rotations), each aligned with the
 learned rotation proposal (the committed network ranks the grid, the exact
 search correlates the best 5%, the exhaustive search is the fallback).  A
@@ -16,19 +16,39 @@ agree on.  A step runs ``Aligner.align_many`` over its pairs: every stage is
 launched for all pairs before the host waits.  The line also reports the
 rate with the global stage (fastVEC, spectra, proposal, global search of
 every pair) replayed as one CUDA graph (``graph_replay``; ``--graph`` makes
-that the headline).  ``--workload pair200_s2_a10``:
-one 200^3 / 100^3 pair per step, exhaustive search (no network).
+that the headline).
+
+At one GPU the same line carries, under ``configs``, the other benchmarked
+configurations, each with its own device-timed value, end-to-end value, FP32
+roofline and CPU baseline (at most 5 timed steps after 3 warm-up steps):
+
+  pair200_s2_a10   one 200^3 / 100^3 pair per step, s = 2, A = 10 (side 75),
+                   exhaustive, modes V, O, C, P and L
+  uneven64_s4_a15  64 pairs of uneven sizes per step, s = 4, A = 15, global
+                   stage as one CUDA graph, per-pair latency p50 / p99
+  prob128_s3_a15   prob-mode alignment of one 128^3 / 64^3 pair with four
+                   probability channels, grids padded to 64^3, A = 15, with
+                   the float32 and the split-BF16 pass B, errors of both
+                   against a float64 restatement
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py --workload pair200_s2_a10 [--mode V|O|C|P|L]   (one config alone)
+  python bench.py --case <name> [arg]                              (profiling case)
 
 ``value``: device-resident maps, K steps timed with CUDA events between a
 barrier + synchronize on both sides, whole-job alignments/s (max over ranks).
-``e2e``: the same steps through ``Aligner.align_host_many`` with the maps copied
+``e2e``: the same steps through the host entry points with the maps copied
 from pinned host memory every step and the results read back.
+Roofline: FP32 CUDA-core throughput of the dominant search pass, algorithmic
+FLOPs (a real 3-D FFT of N points is 2.5 N log2 N, split evenly over its
+three axes; 8 flops per channel and half-spectrum element for the product)
+over the pass's device time, against the FP32 FMA rate measured here.
 ``--impl reference``: the reference algorithm's CPU path on this host's cores
-(the oracle restatement: C fastVEC with OpenMP, numpy/scipy FFT search with
-every core), exhaustive like the reference, timed on a bounded sample of the
-same workload and scaled to a full alignment.
+(the oracle restatement: C fastVEC single-threaded as the reference's serial
+numba loop, numpy whole-array gather and scipy FFTs with every core as the
+reference's threaded FFTW plans), exhaustive like the reference, timed on a
+bounded sample of the headline workload's first pair and scaled to a full
+alignment.
 """
 from __future__ import annotations
 
@@ -49,6 +69,14 @@ WORKLOAD = "prop128_s3_a10"
 METRIC = "map-pair alignments/s: learned-proposal vs exhaustive on GPU at ≥99% top-1 match"
 UNIT = "alignments/s"
 HELD_OUT_SEED0 = 30_000_000     # training used seeds [0, 20000)
+SUB_STEPS, SUB_WARMUP = 5, 3    # timed / warm-up steps of each sub-configuration
+MODE_NAMES = {"V": "VecProduct", "O": "Overlap", "C": "CC", "P": "PCC", "L": "Laplacian"}
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per rotation of the
+# dominant search kernel (pass A of the register two-step passes), mode V, by
+# grid side, from ncu captures of ``bench.py --case search<d>`` (one launch of
+# k_rpass_a at the search's own batch; profiles/k_rpass_a_side<d>_*.md).
+PASS_A_DRAM_PER_ROT = {30: 4426, 75: 4292364}
 
 
 def parse():
@@ -62,6 +90,8 @@ def parse():
     ap.add_argument("--pairs", type=int, default=16, help="pairs per step (prop128_s3_a10)")
     ap.add_argument("--mode", default="V", choices=list("VOCPL"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="headline only (no pair200 / uneven64 / prob128 sub-objects)")
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--no-exhaustive", action="store_true",
                     help="skip the exhaustive form on the same pairs (profiling runs)")
@@ -69,6 +99,8 @@ def parse():
                     help="headline value with the global stage replayed as one CUDA graph")
     ap.add_argument("--no-graph-replay", action="store_true",
                     help="skip the CUDA-graph measurement (profiler launch lists)")
+    ap.add_argument("--case", nargs="+", default=None, metavar="NAME",
+                    help="run one small profiling case of bench_cases.py instead of a workload")
     return ap.parse_args()
 
 
@@ -137,32 +169,126 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def peaks():
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            pk = json.load(f)
-        return float(pk["hbm_gbs"]), "measured"
-    except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback"
+# ---------------------------------------------------------------------------
+# roofline: algorithmic FLOPs of the search passes and the measured FP32 rate
+# ---------------------------------------------------------------------------
+
+def channels(code):
+    """(forward channels, inverse volumes) of a search: V 3/1, O/C/P/L 1/1,
+    prob 7/2 (vector and probability volumes, both needed in either pass)."""
+    if code == 0:
+        return 3, 1
+    if code == 5:
+        return 7, 2
+    return 1, 1
 
 
-def pass_model(dim, mode):
-    """Algorithmic work of each search pass for one rotation (V: 3 channels).
-    FLOPs: a 3-D real FFT of N points is 2.5 N log2 N, split evenly over the
-    three axes; the spectrum product is 8 flops per channel and half-spectrum
-    element.  Bytes: what each pass must read and write in global memory."""
+def pass_flops(dim, code):
+    """Algorithmic FLOPs per rotation of each search pass: FLOP_rot =
+    (C_fwd + C_inv) 2.5 N log2 N + 8 C_fwd Nh + N split over pass A (forward z
+    and y axes), pass B (forward x axis, product, inverse x axis) and pass C
+    (inverse y and z axes, argmax compare)."""
     N = dim ** 3
-    H = dim // 2 + 1
-    Nh = dim * dim * H
-    C = {"V": 3, "prob": 7}.get(mode, 1)
-    G = 2 if mode == "prob" else 1
-    axis = 2.5 * N * np.log2(dim)          # one axis of one real 3-D FFT
+    Nh = dim * dim * (dim // 2 + 1)
+    cf, ci = channels(code)
+    axis = 2.5 * N * np.log2(dim)      # one axis of one real 3-D transform
+    a = cf * 2 * axis
+    b = cf * axis + 8 * cf * Nh + ci * axis
+    c = ci * 2 * axis + N
+    return {"pass_a": a, "pass_b": b, "pass_c": c, "search": a + b + c}
+
+
+_FP32_PEAK = {}
+
+
+def fp32_peak(dev):
+    """Measured FP32 FMA rate of this GPU (TFLOP/s) and its SM count:
+    vesper_fp32_peak_probe over 8 blocks of 256 threads per SM, best of 5
+    timed launches."""
+    import ctypes
+
+    import torch
+    from vesper_python_gb300 import _native
+    if dev.device in _FP32_PEAK:
+        return _FP32_PEAK[dev.device]
+    sms = torch.cuda.get_device_properties(dev.device).multi_processor_count
+    out = torch.zeros(sms * 8, dtype=torch.float32, device=dev.device)
+    flops = ctypes.c_double(0)
+    best = 0.0
+    for i in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _native.check(dev.lib.vesper_fp32_peak_probe(sms * 8, 256, 4096, ctypes.c_void_p(out.data_ptr()),
+                                                     ctypes.byref(flops), dev.stream))
+        e1.record()
+        torch.cuda.synchronize()
+        if i:
+            best = max(best, flops.value / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    _FP32_PEAK[dev.device] = (best, sms)
+    return best, sms
+
+
+def search_roofline(prof, dev, clocks, kernels):
+    """FP32 roofline of the dominant search pass from a profiled step.
+    ``prof`` holds the summed device time and launch count of each pass and
+    every profiled call's (side, mode code, rotations, mixed); ``kernels``
+    names the kernel of each pass.  A fused search (one kernel per call) is
+    reported as a whole."""
+    names = ["pass_a", "pass_b", "pass_c"]
+    flop = {k: 0.0 for k in names + ["search"]}
+    rot_by_side = {}
+    for (d, code, n, _mixed, path) in prof["calls"]:
+        pf = pass_flops(d, code)
+        if path == 2:       # fused: the whole search runs in the pass-A slot
+            pf = {"pass_a": pf["search"], "pass_b": 0.0, "pass_c": 0.0, "search": pf["search"]}
+        for k in flop:
+            flop[k] += pf[k] * n
+        rot_by_side[d] = rot_by_side.get(d, 0) + n
+    ms = prof["pass_ms"][:3]
+    nl = prof["pass_launches"][:3]
+    fused = nl[1] == 0 and nl[2] == 0
+    top = 0 if fused else int(np.argmax(ms))
+    k = "search" if fused else names[top]
+    peak, sms = fp32_peak(dev)
+    sm_mhz = clocks.get("sm_mhz") or 0.0
+    nominal = sms * 128 * 2 * sm_mhz * 1e6 / 1e12 if sm_mhz else None
+    t_top = ms[top] / 1e3
+    ach = flop[k] / t_top / 1e12 if t_top > 0 else 0.0
+    t_all = sum(ms) / 1e3
+    # DRAM bytes per launch of pass A: the measured bytes per rotation at the
+    # searched sides times the rotations of an average launch (mode V; null
+    # when a searched side or mode has no capture)
+    traffic = None
+    codes = {c for (_d, c, _n, _m, _p) in prof["calls"]}
+    if not fused and top == 0 and codes == {0} and all(d in PASS_A_DRAM_PER_ROT for d in rot_by_side):
+        traffic = int(round(sum(PASS_A_DRAM_PER_ROT[d] * n for d, n in rot_by_side.items()) / max(1, nl[0])))
     return {
-        "pass_a": {"flop": C * 2 * axis, "bytes": N * 20 + C * Nh * 8},
-        "pass_b": {"flop": C * axis + 8 * C * Nh + G * axis, "bytes": C * Nh * 8 * 2 + G * Nh * 8},
-        "pass_c": {"flop": G * 2 * axis + N, "bytes": G * Nh * 8},
+        "bound": "fp32", "kernel": f"search {k} ({kernels.get(k, k)})",
+        "achieved": round(ach, 3), "peak": round(peak, 2), "unit": "TFLOP/s", "frac": round(ach / peak, 4),
+        "traffic": traffic, "traffic_unit": "DRAM bytes per launch",
+        "peak_source": f"measured FP32 FMA rate ({sms} SMs, vesper_fp32_peak_probe)",
+        "nominal_tflops_at_sampled_clock": round(nominal, 1) if nominal else None,
+        "flop_per_launch": round(flop[k] / max(1, nl[top])),
+        "launches": int(nl[top]), "ms": round(ms[top], 3),
+        "whole_search": {"achieved": round(flop["search"] / t_all / 1e12, 3) if t_all > 0 else 0.0,
+                         "frac": round(flop["search"] / t_all / 1e12 / peak, 4) if t_all > 0 else 0.0,
+                         "ms": round(sum(ms), 3)},
+        "rotations_by_side": {str(d): n for d, n in sorted(rot_by_side.items())},
     }
 
+
+def kernel_names(dev, dim, mode):
+    from vesper_python_gb300 import vesper as vg
+    path = vg.search_plan(dim, mode, 0, 1, None, dev)[0]
+    if path == 2:
+        return {"search": "k_fused"}
+    pre = "k_rpass_" if path == 1 else "k_pass_"
+    return {"pass_a": pre + "a", "pass_b": pre + "b", "pass_c": pre + "c"}
+
+
+# ---------------------------------------------------------------------------
+# the headline: learned proposal vs exhaustive on the 128^3 / 64^3 pairs
+# ---------------------------------------------------------------------------
 
 def workload_pairs(args, rank, dev):
     """Device maps, pinned host copies and origins of the step's pairs."""
@@ -181,6 +307,25 @@ def workload_pairs(args, rank, dev):
     return pairs
 
 
+def _host_pair(item):
+    """A synth.MapPair of host copies of one (map1, map2, w1, w2, orig1,
+    orig2) item."""
+    from vesper_python_gb300 import synth
+    return synth.MapPair(item[0].cpu().numpy(), item[1].cpu().numpy(), np.asarray(item[4], np.float64),
+                         np.asarray(item[5], np.float64), float(item[2]), None, None)
+
+
+def _gpu_fields(al, item, p):
+    """Host copies of one pair's coarse fields (target data/vec, query
+    data/vec, the target's fastVEC average) as the device path computes
+    them: the inputs of a CPU baseline's search sample."""
+    res = al.align_many([item], p)
+    fl = al.last_fields[0]
+    out = {k: (v.cpu().numpy() if hasattr(v, "cpu") else v) for k, v in fl.items()}
+    out["dim"] = res[0].dim
+    return out
+
+
 def run_gb300(args):
     import torch
     import torch.distributed as dist
@@ -193,7 +338,7 @@ def run_gb300(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     w = synth.WORKLOADS[args.workload]
-    mode = {"V": "VecProduct", "O": "Overlap", "C": "CC", "P": "PCC", "L": "Laplacian"}[args.mode]
+    mode = MODE_NAMES[args.mode]
     dev = vg.Device(f"cuda:{local}")
     use_prop = args.workload == "prop128_s3_a10"
     if use_prop and mode != "VecProduct":
@@ -275,22 +420,27 @@ def run_gb300(args):
     al.align_many(dev_items, p)
     barrier()
     al.profile = None
+
     # ---- end to end: host maps copied in every step -------------------------
     def host_step(params):
         flush.zero_()
         al.align_host_many(host_items, params)
         return al.d2h_bytes
-    host_step(p)
-    barrier()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record()
-    d2h = 0
-    for _ in range(args.steps):
-        d2h += host_step(p)
-    t1.record()
-    barrier()
-    e2e_ms = maxr(t0.elapsed_time(t1))
+
+    def timed_host(params):
+        host_step(params)
+        barrier()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        d2h = 0
+        for _ in range(args.steps):
+            d2h += host_step(params)
+        t1.record()
+        barrier()
+        return maxr(t0.elapsed_time(t1)), d2h
+
+    e2e_ms, d2h = timed_host(p)
     e2e_value = world * npairs * args.steps / (e2e_ms / 1e3)
     h2d = sum(int(h1.numel() * 4 + h2.numel() * 4) for (_, _, h1, h2, _, _, _) in pairs)
     # ---- the exhaustive form on the same pairs --------------------------------
@@ -301,46 +451,19 @@ def run_gb300(args):
         agree_model = sum(int(a.models[0].angle == b.models[0].angle and
                               abs(a.models[0].dot_score - b.models[0].dot_score) <= 1e-4 * abs(b.models[0].dot_score))
                           for a, b in zip(res, res_x))
+        e2e_x, d2h_x = timed_host(p_exh)
         exh = {"value": round(world * npairs * args.steps / (ms_x / 1e3), 4), "unit": UNIT,
                "ms_per_step": round(ms_x / args.steps, 3),
+               "e2e": {"value": round(world * npairs * args.steps / (e2e_x / 1e3), 4), "unit": UNIT,
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(d2h_x / args.steps)},
                "top1_agreement": agree / npairs, "refined_model1_agreement": agree_model / npairs,
                "proposal_speedup": round(ms_x / ms, 3), "proposal_fallbacks_per_step": fallbacks}
-    dim = res[0].dim
+    dims = sorted({r.dim for r in res})
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
-    # ---- roofline of the dominant search pass ---------------------------------
-    pm = pass_model(dim, args.mode)
-    names = ["pass_a", "pass_b", "pass_c"]
-    pass_ms = prof["pass_ms"][:3]
-    pass_n = prof["pass_launches"][:3]
-    top = int(np.argmax(pass_ms))
-    plan_path = vg.search_plan(dim, mode, 0, 1, None, dev)[0]
-    nrot_step = None
-    if use_prop:
-        k = int(np.ceil(0.05 * len(vg.calc_angle_comb(p.A))))
-        nrot_step = npairs * (k + 10 * 27)
-    else:
-        nrot_step = npairs * (len(vg.calc_angle_comb(p.A)) + 10 * 27)
-    per_launch_rot = nrot_step / max(1, pass_n[top])
-    avg_s = pass_ms[top] / max(1, pass_n[top]) / 1e3
-    peak, peak_kind = peaks()
-    ach_bytes = pm[names[top]]["bytes"] * per_launch_rot / avg_s / 1e9
-    ach_flop = pm[names[top]]["flop"] * per_launch_rot / avg_s / 1e12
-    sm_mhz = clocks.get("sm_mhz") or 1900.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    # DRAM bytes of the kernel per launch: the ncu capture's bytes per rotation
-    # (profiles/traffic_<workload>.txt) times the rotations of an average launch
-    traffic = None
-    tr_path = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.txt")
-    if os.path.exists(tr_path) and args.mode == "V":
-        for ln in open(tr_path):
-            f = ln.split()
-            if len(f) == 2 and not ln.startswith("#") and f[0] == names[top]:
-                traffic = int(round(float(f[1]) * per_launch_rot))
-    kname = {0: "k_pass_", 1: "k_rpass_", 2: "k_fused"}[plan_path]
-    kname = kname + names[top][-1] if plan_path != 2 else kname
+    roof = search_roofline(prof, dev, clocks, kernel_names(dev, res[0].dim, mode))
     if use_prop:
         wl = (f"{args.workload}: {npairs} pairs per step, map1 128^3 / map2 64^3 (seeded blob maps, held-out seeds), "
               f"s=3, A=10 (24624 rotations, 5% correlated after the learned proposal, exhaustive fallback) "
@@ -355,7 +478,7 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 fastVEC, target spectra, rescoring; bf16 weights)",
         "data": data,
-        "config": {"workload": wl, "grid_side": dim, "pairs_per_step": npairs,
+        "config": {"workload": wl, "grid_sides": dims, "pairs_per_step": npairs,
                    "rotations": len(vg.calc_angle_comb(p.A)),
                    "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{world}",
                    "global_stage": "one CUDA graph replay per step" if args.graph else "eager launches"},
@@ -365,11 +488,7 @@ def run_gb300(args):
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": f"search {names[top]} ({kname})", "achieved": round(ach_bytes, 1),
-                     "peak": peak, "unit": "GB/s", "frac": round(ach_bytes / peak, 4), "traffic": traffic,
-                     "peak_source": peak_kind,
-                     "fp32": {"achieved_tflops": round(ach_flop, 3), "peak_tflops": round(fp32_peak, 1),
-                              "frac": round(ach_flop / fp32_peak, 4)}},
+        "roofline": roof,
         "stage_ms_profiled_step": {k: round(v, 3) for k, v in stages.items()},
         "pass_ms_profiled_step": [round(x, 3) for x in prof["pass_ms"]],
         "clocks": clocks,
@@ -377,13 +496,107 @@ def run_gb300(args):
     if exh is not None:
         line["exhaustive"] = exh
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args, threads=1, budget_s=12.0)
+        cb = cpu_baseline_exhaustive(args.workload, args.mode, 10.0, _host_pair(dev_items[0]),
+                                     fields=_gpu_fields(al, dev_items[0], p_exh))
+        line["cpu_baseline"] = cb
+        if exh is not None:
+            exh["vs_cpu_baseline"] = round(exh["value"] / cb["value"], 1)
+            exh["e2e_vs_cpu_baseline"] = round(exh["e2e"]["value"] / cb["value"], 1)
+    if world == 1 and use_prop and not args.no_configs:
+        del flush, al
+        torch.cuda.empty_cache()
+        line["configs"] = {
+            "pair200_s2_a10": config_pair200(args, dev),
+            "uneven64_s4_a15": run_uneven(args, sub=True),
+            "prob128_s3_a15": run_prob(args, sub=True),
+        }
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
 
 
-def run_uneven(args):
+# ---------------------------------------------------------------------------
+# configuration 1: the 200^3 / 100^3 pair, all five modes
+# ---------------------------------------------------------------------------
+
+def config_pair200(args, dev):
+    import torch
+
+    from vesper_python_gb300 import align, synth
+    w = synth.WORKLOADS["pair200_s2_a10"]
+    pr = synth.workload_pair("pair200_s2_a10", seed=0)
+    items = [(dev.to_dev(pr.map1), dev.to_dev(pr.map2), pr.width, pr.width, pr.orig1, pr.orig2)]
+    h1, h2 = torch.from_numpy(pr.map1).pin_memory(), torch.from_numpy(pr.map2).pin_memory()
+    host_items = [(h1, h2, pr.width, pr.width, pr.orig1, pr.orig2)]
+    h2d = int(h1.numel() * 4 + h2.numel() * 4)
+    al = align.Aligner(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev.device)
+    steps, warmup = min(args.steps, SUB_STEPS), SUB_WARMUP
+    out = {"config": {"workload": "pair200_s2_a10: one pair per step, map1 200^3 / map2 100^3 (1500 blobs, 70 A "
+                                  "sphere), s=2, A=10 (24624 rotations + refinement), g=16, N=10, exhaustive; "
+                                  "headline fields from mode V",
+                      "l2": "flushed before every step (256 MB write)"},
+           "steps": steps, "warmup": warmup, "unit": UNIT, "modes": {}}
+    fields_v = None
+    for m in "VOCPL":
+        p = align.AlignParams(t=w["t"], T=w["T"], g=w["g"], s=w["s"], A=w["A"], N=w["N"], mode=MODE_NAMES[m])
+        for _ in range(warmup):
+            flush.zero_()
+            al.align_many(items, p)
+        torch.cuda.synchronize()
+        clk = ClockSampler(torch.cuda.current_device())
+        clk.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        total, launches = 0.0, 0
+        for _ in range(steps):
+            flush.zero_()
+            e0.record()
+            res = al.align_many(items, p)
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+            launches += al.launches
+        clocks = clk.stop()
+        prof = {}
+        al.profile = prof
+        al.align_many(items, p)
+        torch.cuda.synchronize()
+        al.profile = None
+        ms = total / steps
+        ent = {"value": round(1e3 / ms, 4), "ms_per_step": round(ms, 3), "gpu_launches_per_step": launches // steps,
+               "grid_side": res[0].dim,
+               "roofline": search_roofline(prof, dev, clocks, kernel_names(dev, res[0].dim, MODE_NAMES[m])),
+               "pass_ms_profiled_step": [round(x, 3) for x in prof["pass_ms"]], "clocks": clocks}
+        if m == "V":
+            al.align_host_many(host_items, p)
+            torch.cuda.synchronize()
+            e0.record()
+            d2h = 0
+            for _ in range(steps):
+                flush.zero_()
+                al.align_host_many(host_items, p)
+                d2h += al.d2h_bytes
+            e1.record()
+            torch.cuda.synchronize()
+            ent["e2e"] = {"value": round(1e3 / (e0.elapsed_time(e1) / steps), 4), "unit": UNIT,
+                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(d2h / steps)}
+            fields_v = _gpu_fields(al, items[0], p)
+        out["modes"][m] = ent
+    v = out["modes"]["V"]
+    out.update({"value": v["value"], "ms_per_step": v["ms_per_step"], "e2e": v["e2e"], "roofline": v["roofline"],
+                "gpu_launches": v["gpu_launches_per_step"] * steps, "clocks": v["clocks"]})
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_exhaustive("pair200_s2_a10", "V", 8.0, pr, fields=fields_v)
+        out["vs_cpu_baseline"] = round(out["value"] / out["cpu_baseline"]["value"], 1)
+        out["e2e_vs_cpu_baseline"] = round(out["e2e"]["value"] / out["cpu_baseline"]["value"], 1)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# configuration 2: 64 pairs of uneven sizes
+# ---------------------------------------------------------------------------
+
+def run_uneven(args, sub=False):
     """64 pairs of uneven sizes (map1 side in {64..256}, map2 = map1 / 2, blob
     count proportional to volume) at s = 4, A = 15, exhaustive search: one
     align_many call per step with the global stage replayed as one CUDA graph.
@@ -396,6 +609,8 @@ def run_uneven(args):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     dev = vg.Device(f"cuda:{local}")
+    steps = min(args.steps, SUB_STEPS) if sub else args.steps
+    warmup = SUB_WARMUP if sub else args.warmup
     w = synth.UNEVEN_WORKLOAD
     p = align.AlignParams(t=w["t"], T=w["T"], g=w["g"], s=w["s"], A=w["A"], N=w["N"])
     items, host_items, sides = [], [], []
@@ -432,11 +647,16 @@ def run_uneven(args):
 
     clk = ClockSampler(local)
     clk.start()
-    ms, lat, launches, res = timed(True, args.steps, args.warmup)
+    ms, lat, launches, res = timed(True, steps, warmup)
     clocks = clk.stop()
-    ms_ng, lat_ng, _, res_ng = timed(False, max(1, args.steps), 1)
+    ms_ng, lat_ng, _, res_ng = timed(False, max(1, steps), 1)
     same = all(a.top == b.top and [m.dot_score for m in a.models] == [m.dot_score for m in b.models]
                for a, b in zip(res, res_ng))
+    prof = {}
+    al.profile = prof
+    al.align_many(items, p)
+    torch.cuda.synchronize()
+    al.profile = None
     # e2e: maps copied from pinned host memory every step
     al.align_host_many(host_items, p, True)
     torch.cuda.synchronize()
@@ -444,13 +664,13 @@ def run_uneven(args):
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record()
     d2h = 0
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.zero_()
         al.align_host_many(host_items, p, True)
         d2h += al.d2h_bytes
     t1.record()
     torch.cuda.synchronize()
-    e2e_ms = t0.elapsed_time(t1) / args.steps
+    e2e_ms = t0.elapsed_time(t1) / steps
     # each pair alone (one align_device per pair); the first pass over the
     # pairs warms the single-pair path (its scratch buffers), the second is timed
     for it in items:
@@ -469,9 +689,13 @@ def run_uneven(args):
     n = len(items)
     dims = sorted({r.dim for r in res})
     pct = lambda a, q: round(float(np.percentile(a, q)), 3)
+    # pass roofline over the whole batch (every side's register / radix-pass
+    # searches; the fused sides' time counts in whole_search only)
+    roof = search_roofline(prof, dev, clocks, {"pass_a": "k_rpass_a / k_pass_a", "pass_b": "k_rpass_b / k_pass_b",
+                                               "pass_c": "k_rpass_c / k_pass_c", "search": "k_fused"})
     line = {
-        "metric": METRIC, "value": round(n / (ms / 1e3), 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": round(n / (ms / 1e3), 4), "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (f64 fastVEC, target spectra, rescoring)",
         "data": "synthetic (seeded blob-map pairs of uneven sizes at 1 A, generated on the GPU)",
         "config": {"workload": f"uneven64_s4_a15: {n} pairs per step, map1 side in {sorted(set(sides))} "
@@ -488,14 +712,28 @@ def run_uneven(args):
         "graph": {"captures": al.graph_captures, "replays": al.graph_replays},
         "e2e": {"value": round(n / (e2e_ms / 1e3), 4), "unit": UNIT,
                 "h2d_bytes_per_step": int(sum(h1.numel() * 4 + h2.numel() * 4 for (h1, h2, *_r) in host_items)),
-                "d2h_bytes_per_step": int(d2h / args.steps)},
+                "d2h_bytes_per_step": int(d2h / steps)},
         "gpu_launches": int(launches),
+        "roofline": roof,
         "clocks": clocks,
     }
-    print(json.dumps(line), flush=True)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_uneven(items, sides, budget_s=8.0)
+        line["vs_cpu_baseline"] = round(line["value"] / line["cpu_baseline"]["value"], 1)
+        line["e2e_vs_cpu_baseline"] = round(line["e2e"]["value"] / line["cpu_baseline"]["value"], 1)
+    if sub:
+        for k in ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline"):
+            line.pop(k)
+        return line
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
-def run_prob(args):
+# ---------------------------------------------------------------------------
+# configuration 3: prob mode at side 64, float32 vs split-BF16 vs float64
+# ---------------------------------------------------------------------------
+
+def run_prob(args, sub=False):
     """prob128_s3_a15: one 128^3 / 64^3 pair with four probability channels
     per step (Dirichlet(0.5) inside the thresholded density, rotated with map2),
     s = 3, grids padded to 64^3, A = 15 (7,488 rotations), alpha = 0.5.  A step
@@ -503,8 +741,11 @@ def run_prob(args):
     the eight probability maps, target spectra, the statistics pass and the
     mixed pass over the grid, top-N, and the mixed pass over the refinement
     set.  Timed with the float32 pass B (headline) and with the split-BF16
-    tensor-core pass B (search path 3); the line reports both and how far the
-    split-BF16 scores are from the float32 ones."""
+    tensor-core pass B (search path 3); the line reports both, how far each
+    form's scores are from a float64 restatement (the oracle with float64
+    FFTs, same gather) on a sample of rotations, and the end-to-end rate with
+    the maps and probability channels copied from pinned host memory and the
+    refined scores read back every step."""
     import contextlib
     import io
 
@@ -515,16 +756,22 @@ def run_prob(args):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     dev = vg.Device(f"cuda:{local}")
+    steps = min(args.steps, SUB_STEPS) if sub else args.steps
+    warmup = SUB_WARMUP if sub else args.warmup
     w = synth.WORKLOADS["prob128_s3_a15"]
     pr = synth.workload_pair("prob128_s3_a15", seed=rank)
     d, s_, g = int(w["pad"]), float(w["s"]), float(w["g"])
     geo = []
+    host_maps = []
     for src, orig, th in ((pr.map1, pr.orig1, w["t"]), (pr.map2, pr.orig2, w["T"])):
         m = vg.mrc_obj.from_array(src, 1.0, orig)
         with contextlib.redirect_stdout(io.StringIO()):
             _, mn = vg.mrc_set_vox_size(m, th, s_)
+        host_maps.append(torch.from_numpy(np.ascontiguousarray(m.data, np.float32)).pin_memory())
         geo.append((dev.to_dev(m.data), np.float64(m.xwidth), m.orig.astype(np.float64),
                     np.asarray(mn.cent, np.float64) - 0.5 * s_ * d))
+    host_probs = [torch.from_numpy(np.ascontiguousarray(np.moveaxis(pm, 3, 0), np.float32)).pin_memory()
+                  for pm in (pr.prob1, pr.prob2)]
     pmaps = [[dev.to_dev(np.ascontiguousarray(pm[..., k], np.float32)) for k in range(4)]
              for pm in (pr.prob1, pr.prob2)]
     angles = vg.calc_angle_comb(w["A"])
@@ -532,41 +779,51 @@ def run_prob(args):
     n = len(angles)
     rd3 = 1.0 / d ** 3
     alpha = float(w["alpha"])
+    dsrc = [torch.empty_like(geo[i][0]) for i in range(2)]
+    dprob = [torch.empty(tuple(host_probs[i].shape), dtype=torch.float32, device=dev.device) for i in range(2)]
 
-    def fields(i):
+    def fields(i, from_host):
         # prob mode keeps fastVEC's density in float32 (main.py:345)
         src, sw, so, no = geo[i]
+        pm = pmaps[i]
+        if from_host:
+            dsrc[i].copy_(host_maps[i], non_blocking=True)
+            dprob[i].copy_(host_probs[i], non_blocking=True)
+            src, pm = dsrc[i], [dprob[i][k] for k in range(4)]
         _, d32, vec = vg.fastvec_device(src, sw, so, d, s_, no, g, dev=dev)
-        probs = torch.stack([vg.fastvec_device(pm, sw, so, d, s_, no, g, dev=dev)[1] for pm in pmaps[i]])
+        probs = torch.stack([vg.fastvec_device(p_, sw, so, d, s_, no, g, dev=dev)[1] for p_ in pm])
         return d32.double(), vec, probs
 
-    def step(path):
+    def step(path, from_host=False, prof=None):
         opts = (path, 0, 0)
-        tdata, tvec, tprobs = fields(0)
-        qdata, qvec, qprobs = fields(1)
+        tdata, tvec, tprobs = fields(0, from_host)
+        qdata, qvec, qprobs = fields(1, from_host)
         spec = vg.target_spectra_device(tdata, tvec, "prob", 0.0, probs=tprobs, dev=dev)
-        s1, _ = vg.search_device(spec, qdata, qvec, "prob", 0.0, mats, probs=qprobs, dev=dev, opts=opts)
+        s1, _ = vg.search_device(spec, qdata, qvec, "prob", 0.0, mats, probs=qprobs, dev=dev, opts=opts,
+                                 profile=prof)
         h = s1.cpu().numpy().astype(np.float64) * rd3
         mix = (alpha, float(np.std(h[:, 0])), float(np.mean(h[:, 0])), float(np.std(h[:, 1])),
                float(np.mean(h[:, 1])))
-        s2, l2 = vg.search_device(spec, qdata, qvec, "prob", 0.0, mats, probs=qprobs, mix=mix, dev=dev, opts=opts)
+        s2, l2 = vg.search_device(spec, qdata, qvec, "prob", 0.0, mats, probs=qprobs, mix=mix, dev=dev, opts=opts,
+                                  profile=prof)
         top = [int(t) for t in vg.topn_device(s2, w["N"], column=2, dev=dev).cpu().numpy() if t >= 0]
         ref = vg.refine_angle_list([angles[t] for t in top])
         rs, rl = vg.search_device(spec, qdata, qvec, "prob", 0.0, dev.to_dev(vg.rot_matrices(ref)), probs=qprobs,
-                                  mix=mix, dev=dev, opts=opts)
+                                  mix=mix, dev=dev, opts=opts, profile=prof)
         rtop = [int(t) for t in vg.topn_device(rs, w["N"], column=2, dev=dev).cpu().numpy() if t >= 0]
-        return s1, s2, top, rtop
+        rsc = rs[rtop].cpu().numpy()          # the refined models' scores (read back)
+        return s1, s2, top, rtop, mix, rsc, (tdata, tvec, tprobs, qdata, qvec, qprobs)
 
     out = {}
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev.device)
     for path in (-1, 3):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             res = step(path)
         torch.cuda.synchronize()
         clk = ClockSampler(local)
         clk.start()
         total = 0.0
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
@@ -574,15 +831,33 @@ def run_prob(args):
             e1.record()
             torch.cuda.synchronize()
             total += e0.elapsed_time(e1)
-        out[path] = (total / args.steps, res, clk.stop())
-    ms, (s1, s2, top, rtop), clocks = out[-1]
-    ms3, (t1, t2, ttop, trtop), _ = out[3]
+        out[path] = (total / steps, res, clk.stop())
+    ms, (s1, s2, top, rtop, mix, _, flds), clocks = out[-1]
+    ms3, (t1, t2, ttop, trtop, _, _, _), _ = out[3]
+    # end to end: maps and probability channels from pinned host memory
+    step(-1, from_host=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        flush.zero_()
+        step(-1, from_host=True)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / steps
+    h2d = int(sum(t.numel() * 4 for t in host_maps + host_probs))
+    # statistics-pass scores, both top-N lists, the refined models' scores
+    d2h = int(n * 2 * 4 + 2 * w["N"] * 4 + w["N"] * 3 * 4)
+    prof = {}
+    step(-1, prof=prof)
+    torch.cuda.synchronize()
+    roof = search_roofline(prof, dev, clocks, kernel_names(dev, d, "prob"))
     a1, b1 = s1.cpu().numpy().astype(np.float64), t1.cpu().numpy().astype(np.float64)
     a2, b2 = s2.cpu().numpy().astype(np.float64), t2.cpu().numpy().astype(np.float64)
-    rel = lambda x, y: float(np.max(np.abs(x - y)) / max(np.max(np.abs(x)), 1e-300))
+    rel = lambda x, y: float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
     line = {
         "metric": "prob-mode map-pair alignments/s", "value": round(1e3 / ms, 4), "unit": "alignments/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "n_gpus": world, "steps": steps, "warmup": warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 FFT (f64 target spectra); split-BF16 pass B in the comparison",
         "data": "synthetic (seeded 128^3 / 64^3 blob-map pair at 1 A, 4 Dirichlet(0.5) probability channels)",
@@ -591,80 +866,234 @@ def run_prob(args):
                                f"g={g}, N={w['N']}; fastVEC of the densities and the 8 probability maps in the step",
                    "grid_side": d, "l2": "flushed before every step (256 MB write)",
                    "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(1e3 / e2e_ms, 4), "unit": "alignments/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": roof,
         "split_bf16_pass_b": {"value": round(1e3 / ms3, 4), "ms_per_step": round(ms3, 3),
-                              "max_rel_diff_vs_f32": {"vec_score": rel(a1[:, 0], b1[:, 0]),
-                                                      "prob_score": rel(a1[:, 1], b1[:, 1]),
-                                                      "mixed_score": rel(a2[:, 2], b2[:, 2])},
+                              "max_rel_diff_vs_f32": {"vec_score": rel(b1[:, 0], a1[:, 0]),
+                                                      "prob_score": rel(b1[:, 1], a1[:, 1]),
+                                                      "mixed_score": rel(b2[:, 2], a2[:, 2])},
                               "top_n_same": top == ttop, "refined_top_n_same": rtop == trtop},
+        "vs_fp64": prob_fp64_errors(flds, angles, mix, a1, b1, a2, b2),
         "clocks": clocks,
     }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_prob(flds, geo, pmaps, d, s_, g, n, budget_s=8.0)
+        line["vs_cpu_baseline"] = round(line["value"] / line["cpu_baseline"]["value"], 1)
+        line["e2e_vs_cpu_baseline"] = round(line["e2e"]["value"] / line["cpu_baseline"]["value"], 1)
+    if sub:
+        for k in ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline"):
+            line.pop(k)
+        return line
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
-
-
-def cpu_baseline(args, threads, budget_s):
-    """The reference algorithm on this host's CPU (the oracle restatement,
-    exhaustive search like the reference), timed on a bounded sample and
-    scaled to one full alignment."""
+def prob_fp64_errors(flds, angles, mix, a1, b1, a2, b2, nsample=12):
+    """Errors of the float32 and split-BF16 scores against the oracle with
+    float64 FFTs (same gather, same statistics) on ``nsample`` rotations
+    spread over the grid, relative to the largest float64 score of each kind."""
     from oracle import vesper_oracle as orc
-    from vesper_python_gb300 import synth
-    w = synth.WORKLOADS[args.workload]
-    if args.workload == "prop128_s3_a10":
-        pair = synth.make_pair(HELD_OUT_SEED0, w["side1"], w["nblob"], w["radius"])
-    else:
-        pair = synth.workload_pair(args.workload, seed=0)
-    m1 = orc.OMap(pair.map1, 1.0, pair.orig1)
-    m2 = orc.OMap(pair.map2, 1.0, pair.orig2)
-    d1, o1, c1, _ = orc.set_vox_size(m1, w["t"], w["s"])
-    d2, o2, c2, _ = orc.set_vox_size(m2, w["T"], w["s"])
-    dim, o1, o2 = orc.unify(d1, o1, c1, d2, o2, c2, w["s"])
-    rng = np.random.default_rng(0)
+    td, tv, tp, qd, qv, qp = [t.cpu().numpy() for t in flds]
+    tspec = orc.target_spectra([tv[..., 0], tv[..., 1], tv[..., 2]] + list(tp))
+    sel = np.linspace(0, len(angles) - 1, nsample).astype(int)
+    st = (mix[1], mix[2], mix[3], mix[4])
+    r = [orc.rot_and_search_prob(tspec, qd.astype(np.float32), qv, list(qp), angles[i], mix[0], st, fp64=True)
+         for i in sel]
+    ref = np.array([[x[0], x[2], x[4]] for x in r], np.float64)
+    out = {}
+    for name, s_1, s_2 in (("f32", a1, a2), ("split_bf16", b1, b2)):
+        got = np.stack([s_1[sel, 0], s_1[sel, 1], s_2[sel, 2]], axis=1)
+        err = np.max(np.abs(got - ref), axis=0) / np.max(np.abs(ref), axis=0)
+        out[name] = {"vec_score": float(err[0]), "prob_score": float(err[1]), "mixed_score": float(err[2])}
+    out["rotations"] = int(nsample)
+    out["note"] = "max |score - float64 score| / max |float64 score| over the sampled rotations"
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU baselines: the reference algorithm on the host cores (oracle port)
+# ---------------------------------------------------------------------------
+
+def _cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def _fastvec_sample_seconds(src, width, orig, dim, s, dest_orig, g, nsamp, rng):
+    """Single-threaded C fastVEC (the reference's serial numba loop) on
+    ``nsamp`` random destination voxels, scaled to the whole grid."""
+    from oracle import vesper_oracle as orc
     nvox = dim ** 3
-    nsamp = 600 if threads == 1 else 600 * threads
-    # fastVEC sample: random destination voxels of both maps
-    t_fv = 0.0
-    for m, o in ((m1, o1), (m2, o2)):
-        idx = rng.choice(nvox, size=min(nsamp, nvox), replace=False)
-        t0 = time.perf_counter()
-        orc.fastvec(m.data, np.float64(m.xwidth), m.orig.astype(np.float64), dim, w["s"], o, w["g"], idx=idx,
-                    nthreads=threads)
-        t_fv += (time.perf_counter() - t0) * nvox / len(idx)
-    # search sample: the rotation loop on real fields
-    data1, vec1 = orc.fastvec(m1.data, np.float64(m1.xwidth), m1.orig.astype(np.float64), dim, w["s"], o1, w["g"],
-                              idx=np.arange(0), nthreads=threads)
-    rngv = np.random.default_rng(1)
-    vec1 = rngv.normal(size=vec1.shape).astype(np.float32)
-    data2 = np.where(rngv.random((dim,) * 3) < 0.3, rngv.uniform(0.5, 2, (dim,) * 3), 0.0)
-    vec2 = rngv.normal(size=vec1.shape).astype(np.float32)
-    ts = orc.target_spectra(orc.mode_field("V", data1, vec1))
-    angles = orc.calc_angle_comb(w["A"])
-    R = len(angles) + 10 * 27
+    idx = rng.choice(nvox, size=min(nsamp, nvox), replace=False)
+    t0 = time.perf_counter()
+    orc.fastvec(src, np.float64(width), np.asarray(orig, np.float64), dim, s, dest_orig, g, idx=idx, nthreads=1)
+    return (time.perf_counter() - t0) * nvox / len(idx)
+
+
+def _search_rotation_seconds(mode, tdata, tvec, qdata, qvec, ave, angles, budget_s, threads, max_rot=200):
+    """Average seconds per rotation of the reference's per-rotation work:
+    numpy whole-array gather, scipy FFTs with ``threads`` workers (the
+    reference's threaded FFTW plans), product, inverse, argmax."""
+    from oracle import vesper_oracle as orc
+    ts = orc.target_spectra(orc.mode_field(mode, tdata, tvec, ave))
     t0 = time.perf_counter()
     n = 0
     while True:
-        orc.rot_and_search(ts, "V", data2, vec2, angles[n * 997 % len(angles)], 0.0, workers=threads)
+        F = orc.rot_matrix_f32(angles[n * 997 % len(angles)])
+        nv, nd = orc.rot_mrc_numpy(qdata, qvec, F)
+        orc.best_trans(orc.correlate(ts, orc.mode_field(mode, nd, nv, ave), workers=threads))
         n += 1
-        if time.perf_counter() - t0 > budget_s * 0.5 or n >= 200:
+        if time.perf_counter() - t0 > budget_s or n >= max_rot:
             break
-    t_rot = (time.perf_counter() - t0) / n
+    return (time.perf_counter() - t0) / n, n
+
+
+def _oracle_grid(w, pair):
+    """Thresholded maps, the unified grid side and both grid origins."""
+    from oracle import vesper_oracle as orc
+    m1 = orc.OMap(pair.map1, pair.width, pair.orig1)
+    m2 = orc.OMap(pair.map2, pair.width, pair.orig2)
+    d1, o1, c1, _ = orc.set_vox_size(m1, w["t"], w["s"])
+    d2, o2, c2, _ = orc.set_vox_size(m2, w["T"], w["s"])
+    dim, o1, o2 = orc.unify(d1, o1, c1, d2, o2, c2, w["s"])
+    return m1, o1, m2, o2, dim
+
+
+def _oracle_fields(w, pair):
+    """Coarse fields of a pair by the oracle (C fastVEC on every core)."""
+    from oracle import vesper_oracle as orc
+    m1, o1, m2, o2, dim = _oracle_grid(w, pair)
+    data1, vec1 = orc.fastvec(m1.data, np.float64(m1.xwidth), m1.orig.astype(np.float64), dim, w["s"], o1, w["g"])
+    data2, vec2 = orc.fastvec(m2.data, np.float64(m2.xwidth), m2.orig.astype(np.float64), dim, w["s"], o2, w["g"])
+    return {"tdata": data1, "tvec": vec1, "qdata": data2, "qvec": vec2,
+            "ave": float(np.mean(data1[data1 > 0])), "dim": dim}
+
+
+def cpu_baseline_exhaustive(workload, mode_letter, budget_s, pair, fields=None):
+    """One exhaustive alignment of ``pair`` on the CPU (oracle port):
+    single-threaded fastVEC of both maps on random voxels, plus the rotation
+    loop on the pair's real fastVEC fields with scipy FFT workers on every
+    core, timed on a sample of rotations and scaled to the grid and the
+    refinement set."""
+    from oracle import vesper_oracle as orc
+    from vesper_python_gb300 import synth
+    w = synth.WORKLOADS[workload]
+    threads = _cores()
+    if fields is None:
+        fields = _oracle_fields(w, pair)
+    m1, o1, m2, o2, dim = _oracle_grid(w, pair)
+    rng = np.random.default_rng(0)
+    nsamp = 400
+    t_fv = sum(_fastvec_sample_seconds(m.data, m.xwidth, m.orig, dim, w["s"], o, w["g"], nsamp, rng)
+               for m, o in ((m1, o1), (m2, o2)))
+    angles = orc.calc_angle_comb(w["A"])
+    R = len(angles) + w["N"] * 27
+    t_rot, n = _search_rotation_seconds(mode_letter, fields["tdata"], fields["tvec"], fields["qdata"],
+                                        fields["qvec"], fields.get("ave", 0.0), angles, budget_s * 0.6, threads)
     total = t_fv + R * t_rot
     return {"value": round(1.0 / total, 6), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{args.workload}: fastVEC on {nsamp} random voxels per map (scaled to {nvox}), exhaustive "
-                      f"search on {n} rotations (scaled to {R}); {t_fv:.1f} s fastVEC + {R * t_rot:.1f} s search "
-                      f"per alignment",
+            "sample": f"{workload} first pair (grid side {dim}), mode {mode_letter}: fastVEC of both maps on "
+                      f"{nsamp} random voxels each, 1 thread (the reference's serial numba loop), scaled to "
+                      f"{dim ** 3} voxels; exhaustive search on the pair's real fastVEC fields, {n} rotations "
+                      f"(numpy whole-array gather, scipy FFTs with {threads} workers), scaled to {R} rotations "
+                      f"(grid + refinement); {t_fv:.1f} s fastVEC + {R * t_rot:.1f} s search per alignment",
+            "seconds_per_alignment": round(total, 2)}
+
+
+def cpu_baseline_uneven(items, sides, budget_s):
+    """The uneven batch on the CPU (oracle port): every 8th pair's fastVEC
+    (random voxels, 1 thread) and rotation loop (sampled, every core) timed
+    and scaled to its own grid; the batch's time = 64 x their mean."""
+    from oracle import vesper_oracle as orc
+    from vesper_python_gb300 import synth
+    w = synth.UNEVEN_WORKLOAD
+    threads = _cores()
+    rng = np.random.default_rng(0)
+    angles = orc.calc_angle_comb(w["A"])
+    R = len(angles) + w["N"] * 27
+    per_pair = []
+    sel = list(range(0, len(items), 8))
+    for i in sel:
+        pair = _host_pair(items[i])
+        f = _oracle_fields(w, pair)
+        m1, o1, m2, o2, dim = _oracle_grid(w, pair)
+        t_fv = sum(_fastvec_sample_seconds(m.data, m.xwidth, m.orig, dim, w["s"], o, w["g"], 60, rng)
+                   for m, o in ((m1, o1), (m2, o2)))
+        t_rot, _ = _search_rotation_seconds("V", f["tdata"], f["tvec"], f["qdata"], f["qvec"], 0.0, angles,
+                                            budget_s * 0.6 / len(sel), threads, max_rot=40)
+        per_pair.append(t_fv + R * t_rot)
+    total = len(items) * float(np.mean(per_pair))
+    return {"value": round(len(items) / total, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"uneven64_s4_a15: {len(sel)} of the {len(items)} pairs (every 8th, map1 sides "
+                      f"{[sides[i] for i in sel]}): fastVEC on 60 random voxels per map (1 thread) and the "
+                      f"rotation loop on the pair's real fastVEC fields (numpy gather, scipy FFTs with {threads} "
+                      f"workers), each scaled to its grid and {R} rotations; batch = {len(items)} x their mean "
+                      f"({total:.0f} s)",
+            "seconds_per_alignment": round(total / len(items), 2)}
+
+
+def cpu_baseline_prob(flds, geo, pmaps, d, s_, g, nrot, budget_s):
+    """The prob-mode alignment on the CPU (oracle port): fastVEC of the two
+    densities and eight probability maps on random voxels (1 thread), and the
+    per-rotation prob search (numpy gather with per-channel masks, 7 forward
+    and 2 inverse scipy FFTs with every core) on the pair's real fields,
+    sampled and scaled to both passes and the refinement set."""
+    from oracle import vesper_oracle as orc
+    threads = _cores()
+    rng = np.random.default_rng(0)
+    nsamp = 60
+    t_fv = 0.0
+    for i in range(2):
+        src, sw, so, no = geo[i]
+        t_fv += _fastvec_sample_seconds(src.cpu().numpy(), sw, so, d, s_, no, g, nsamp, rng)
+        for pm in pmaps[i]:
+            t_fv += _fastvec_sample_seconds(pm.cpu().numpy(), sw, so, d, s_, no, g, nsamp, rng)
+    td, tv, tp, qd, qv, qp = [t.cpu().numpy() for t in flds]
+    qd = qd.astype(np.float32)
+    tspec = orc.target_spectra([tv[..., 0], tv[..., 1], tv[..., 2]] + list(tp))
+    angles = orc.calc_angle_comb(15.0)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        F = orc.rot_matrix_f32(angles[n * 997 % len(angles)])
+        nv, nd, ps = orc.rot_mrc_numpy(qd, qv, F, list(qp))
+        cv = orc.correlate(tspec[:3], [nv[..., 0], nv[..., 1], nv[..., 2]], workers=threads)
+        cp = orc.correlate(tspec[3:], ps, workers=threads)
+        orc.best_trans(cv)
+        orc.best_trans(cp)
+        n += 1
+        if time.perf_counter() - t0 > budget_s * 0.6 or n >= 100:
+            break
+    t_rot = (time.perf_counter() - t0) / n
+    R = 2 * nrot + 270
+    total = t_fv + R * t_rot
+    return {"value": round(1.0 / total, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"prob128_s3_a15: fastVEC of 2 densities + 8 probability maps on {nsamp} random voxels each "
+                      f"(1 thread), scaled to {d}^3; prob rotation search on the pair's real fields, {n} rotations "
+                      f"(numpy gather, 7 forward + 2 inverse scipy FFTs with {threads} workers), scaled to {R} "
+                      f"(both passes + refinement); {t_fv:.1f} s fastVEC + {R * t_rot:.1f} s search per alignment",
             "seconds_per_alignment": round(total, 2)}
 
 
 def run_reference(args):
+    """The reference algorithm on this host's CPU cores (oracle port),
+    exhaustive like the reference, on the headline workload's first pair:
+    each step times a bounded sample and scales it to one alignment."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
+    from vesper_python_gb300 import synth
+    w = synth.WORKLOADS[args.workload]
+    pair = synth.make_pair(HELD_OUT_SEED0, w["side1"], w["nblob"], w["radius"]) \
+        if args.workload == "prop128_s3_a10" else synth.workload_pair(args.workload, seed=0)
+    fields = _oracle_fields(w, pair)
     vals = []
+    cb = None
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(args, threads=threads, budget_s=4.0)
+        cb = cpu_baseline_exhaustive(args.workload, args.mode, 3.0, pair, fields=fields)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.mean(vals))
@@ -674,7 +1103,7 @@ def run_reference(args):
             "data": "synthetic (seeded blob-map pairs at 1 A)",
             "config": {"workload": f"{args.workload}: CPU restatement of the reference path (exhaustive search), "
                                    f"mode {args.mode}"},
-            "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": cb["cores"], "kind": "port",
                              "sample": cb["sample"]},
             "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -682,7 +1111,10 @@ def run_reference(args):
 
 if __name__ == "__main__":
     a = parse()
-    if a.impl == "reference":
+    if a.case:
+        import bench_cases
+        bench_cases.main(a.case)
+    elif a.impl == "reference":
         run_reference(a)
     elif a.workload == "uneven64_s4_a15":
         run_uneven(a)

@@ -250,6 +250,43 @@ def rot_mrc_prob(data, vec, p1, p2, p3, p4, angle, F=None):
     return (ov, od.astype(data.dtype), *ops)
 
 
+def rot_mrc_numpy(data, vec, F, probs=None):
+    """rot_mrc / rot_mrc_prob (VESPER_1_prob_new.py:279-354, :1211-1299) in
+    whole-array numpy operations, the form the reference runs: float32 matmul
+    of the centred new positions by the transposed matrix, in-bounds mask,
+    truncation, density (or per-channel) non-zero mask, fancy-index gather,
+    float32 matmul of the vectors, fancy-index scatter (rows in the
+    reference's order, z slowest, x middle, y fastest, so the last row wins a
+    collision).  For the CPU-baseline timing; the C gather above is the
+    checked form.  Returns (new_vec, new_data[, new_probs list])."""
+    d = vec.shape[0]
+    cent = 0.5 * float(d)
+    ar = np.arange(d)
+    z, x, y = np.meshgrid(ar, ar, ar, indexing="ij")
+    new_pos = np.stack([x.reshape(-1), y.reshape(-1), z.reshape(-1)], axis=1) - cent
+    Ff = np.asarray(F, np.float32)
+    old = new_pos.astype(np.float32) @ Ff.T + np.float32(cent)
+    inb = np.all((old >= 0) & (old < d), axis=1)
+    src = old[inb].astype(np.int32)
+    dst = (new_pos[inb].astype(np.int32) + cent).astype(np.int64)
+    si, sj, sk = src[:, 0], src[:, 1], src[:, 2]
+    di, dj, dk = dst[:, 0], dst[:, 1], dst[:, 2]
+    keep = data[si, sj, sk] != 0.0
+    new_vec = np.zeros_like(vec)
+    new_data = np.zeros_like(data)
+    new_vec[di[keep], dj[keep], dk[keep]] = vec[si[keep], sj[keep], sk[keep]].astype(np.float32) @ Ff
+    new_data[di[keep], dj[keep], dk[keep]] = data[si[keep], sj[keep], sk[keep]]
+    if probs is None:
+        return new_vec, new_data
+    outs = []
+    for p in probs:
+        m = p[si, sj, sk] != 0.0
+        o = np.zeros_like(p)
+        o[di[m], dj[m], dk[m]] = p[si[m], sj[m], sk[m]]
+        outs.append(o)
+    return new_vec, new_data, outs
+
+
 def rot_positions(d, F):
     """float32 old positions and destination indices of every new_pos row."""
     n = d ** 3

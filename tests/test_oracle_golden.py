@@ -63,6 +63,23 @@ def test_rot_mrc_prob(golden_dir, d):
         assert digest(*orc.rot_mrc_prob(data, vec, *probs, a)) == dg
 
 
+@pytest.mark.parametrize("d", [9, 12])
+def test_rot_mrc_numpy_form_matches_reference(golden_dir, d):
+    """The whole-array numpy gather timed by the CPU baseline gives the
+    reference's outputs (digests over every rotation of the 30-degree grid,
+    odd side included; prob channels with their own masks)."""
+    g = _g(golden_dir, "rot_small.npz")
+    data, vec = g[f"d{d}_data"], g[f"d{d}_vec"]
+    ang = orc.calc_angle_comb(30.0)
+    dig = g[f"d{d}_digest"]
+    bad = [r for r, a in enumerate(ang) if digest(*orc.rot_mrc_numpy(data, vec, orc.rot_matrix_f32(a))) != dig[r]]
+    assert not bad
+    data, vec, probs = g[f"p{d}_data"], g[f"p{d}_vec"], g[f"p{d}_probs"]
+    for a, dg in zip(ang[::11], g[f"p{d}_digest"]):
+        nv, nd, ps = orc.rot_mrc_numpy(data, vec, orc.rot_matrix_f32(a), list(probs))
+        assert digest(nv, nd, *ps) == dg
+
+
 def test_odd_side_collision_rule():
     """Odd d: destination index (d-1)/2 takes the later of two source rows and
     the last plane stays empty (identity rotation)."""

@@ -102,6 +102,7 @@ SIGNATURES = {
     "vesper_last_error": [],
     "vesper_max_dim": [_i],
     "vesper_fast_len_ok": [_i],
+    "vesper_fp32_peak_probe": [_i, _i, _i, _vp, _vp, _vp],
     "vesper_prepare_map": [_vp, _i, _i, _i, _d, _vp, _vp, _vp],
     "vesper_map_stats": [_vp, _i, _vp, _vp],
     "vesper_map_stats_workspace_size": [_i, _psz],

@@ -151,8 +151,13 @@ class _Pair:
 class Aligner:
     """Holds the device, cached angle-grid matrices and scratch buffers."""
 
-    def __init__(self, dev: vg.Device | None = None):
+    def __init__(self, dev: vg.Device | None = None, group=None):
         self.dev = dev or vg.default_device()
+        # torch.distributed process group: with one, every search splits its
+        # rotations across the group's ranks (one GPU each) and gathers the
+        # per-rotation results (vg.search_device_sharded); the CUDA-graph form
+        # is then not used (the gather is a host exchange)
+        self.group = group
         self.lib = self.dev.lib
         self.launches = 0
         self.d2h_bytes = 0
@@ -234,7 +239,7 @@ class Aligner:
         # ---- 2-3. fastVEC, statistics, spectra, global pass (one CUDA graph per
         # batch signature when graph=True: the stage needs no host value
         # between its launches except in modes CC/PCC) --------------------------
-        if graph and mode not in ("PCC", "CC"):
+        if graph and mode not in ("PCC", "CC") and self.group is None:
             stats, sh = self._global_stage_graph(P, p, mats, nang), None
         else:
             stats, sh = self._global_stage(P, p, mats, nang)
@@ -313,8 +318,8 @@ class Aligner:
                 sel = inv_all[ioff:ioff + len(ra)]
                 off += nu
                 ioff += len(ra)
-                rs, rl = vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats, batch=p.batch, dev=dev,
-                                          tuned=True)
+                rs, rl = vg.search_device_sharded(st.spec, st.qdata, st.qvec, mode, st.ave, rmats, self.group,
+                                                  batch=p.batch, dev=dev, tuned=True)
                 st.launches += self._search_launches(st.dim, mode, nu, p.batch)
                 st.rs, st.rl = rs.index_select(0, sel), rl.index_select(0, sel)
                 st.rtop = vg.topn_device(st.rs, p.N, dev=dev)
@@ -377,6 +382,11 @@ class Aligner:
                                         float(rh[k, 4]), (st.c1, st.c2, p.s, st.dim)))
             self.launches += st.launches
             out.append(AlignResult(st.dim, st.std_s, st.ave_s, st.top_list, models, st.launches))
+        # the coarse fields of each pair (device tensors), for callers that
+        # score or inspect them further
+        self.last_fields = [{"tdata": getattr(st, "tdata", None), "tvec": getattr(st, "tvec", None),
+                             "qdata": getattr(st, "qdata", None), "qvec": getattr(st, "qvec", None),
+                             "ave": float(getattr(st, "ave", 0.0))} for st in P]
         self._mark("end")
         self._close_marks()
         return out
@@ -570,8 +580,17 @@ class Aligner:
         """Search of the given rotations, top-N and (subset searches, unless
         the caller batches it) the z-score of the best exact score over the
         subset; all on the device."""
-        st.scores, st.lin = vg.search_device(st.spec, st.qdata, st.qvec, p.mode, st.ave, mats, batch=p.batch,
-                                             dev=self.dev, profile=self.profile, tuned=True, out=out)
+        if self.group is not None:
+            sc, ln = vg.search_device_sharded(st.spec, st.qdata, st.qvec, p.mode, st.ave, mats, self.group,
+                                              batch=p.batch, dev=self.dev, tuned=True)
+            if out is not None:
+                out[0].copy_(sc)
+                out[1].copy_(ln)
+                sc, ln = out
+            st.scores, st.lin = sc, ln
+        else:
+            st.scores, st.lin = vg.search_device(st.spec, st.qdata, st.qvec, p.mode, st.ave, mats, batch=p.batch,
+                                                 dev=self.dev, profile=self.profile, tuned=True, out=out)
         st.launches += self._search_launches(st.dim, p.mode, int(mats.shape[0]), p.batch)
         st.top = vg.topn_device(st.scores, p.N, dev=self.dev)
         st.launches += 1

@@ -70,3 +70,37 @@ extern "C" int vesper_fast_len_ok(int n) {
     vg::FftPlan p;
     return (n >= 2 && vg::make_plan(n, &p)) ? 1 : 0;
 }
+
+// ---------------------------------------------------------------------------
+// FP32 FMA throughput probe: the measured denominator of the search kernels'
+// FP32 roofline.  Every thread runs kChains independent fmaf chains for
+// ``iters`` steps (2 flops each); the sum is stored only when it equals a
+// value no chain reaches, so the chains stay live without a store per thread.
+// ---------------------------------------------------------------------------
+namespace vg {
+constexpr int kChains = 16;
+
+__global__ void k_fma_peak(float *out, int iters) {
+    float a[kChains];
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) a[k] = (threadIdx.x + 1) * 1e-6f + k * 1e-7f;
+    const float b = 0.999999f, c = 1e-7f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < kChains; ++k) a[k] = fmaf(a[k], b, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) s += a[k];
+    if (s == -1.0f) out[blockIdx.x] = s;
+}
+}  // namespace vg
+
+extern "C" int vesper_fp32_peak_probe(int blocks, int threads, int iters, float *out, double *flops_out,
+                                      void *stream) {
+    if (blocks < 1 || threads < 32 || threads > 1024 || threads % 32 || iters < 1 || !out || !flops_out)
+        return vg::fail(VESPER_ERR_INVALID, "vesper_fp32_peak_probe: bad arguments");
+    vg::k_fma_peak<<<blocks, threads, 0, (cudaStream_t)stream>>>(out, iters);
+    *flops_out = 2.0 * vg::kChains * (double)iters * threads * blocks;
+    return vg::cuda_check("k_fma_peak");
+}

@@ -2,8 +2,10 @@
 
 Rotations are independent, so rank k searches a contiguous block of the
 rotation grid and keeps its per-rotation (score, translation); there is no
-exchange inside the search.  Two small host exchanges rebuild exactly what a
-single process computes:
+exchange inside the search.  ``search_sharded`` (used by search_map_fft,
+search_map_fft_prob and Aligner.align_many when given a process group)
+gathers the blocks' results in rotation order.  Two small host exchanges
+rebuild exactly what a single process computes:
 
 * top-N: every rank contributes its local stable top-N as
   (score, global rotation index); the merge orders by score descending, then
@@ -56,6 +58,18 @@ def gather_scores(scores: np.ndarray, group=None) -> np.ndarray:
     parts = [None] * world
     dist.all_gather_object(parts, np.asarray(scores), group=group)
     return np.concatenate(parts)
+
+
+def search_sharded(search_block, nrot: int, group=None):
+    """Split ``nrot`` rotations over the ranks of ``group``: this rank runs
+    ``search_block(lo, hi)`` on its block [lo, hi) (returning host arrays
+    scores [hi-lo][nscore], lin [hi-lo][nscore]), then every rank receives
+    all ranks' results in rotation order -- the arrays one process would have
+    computed, so top-N, statistics and refinement proceed unchanged."""
+    import torch.distributed as dist
+    lo, hi = shard_range(nrot, dist.get_rank(group), dist.get_world_size(group))
+    sc, ln = search_block(lo, hi)
+    return gather_scores(sc, group), gather_scores(ln, group)
 
 
 def prob_stats(vscores_scaled: np.ndarray, pscores_scaled: np.ndarray):

@@ -487,11 +487,39 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
         for k in range(4):
             profile.setdefault("pass_ms", [0.0] * 4)[k] += ms[k]
             profile.setdefault("pass_launches", [0] * 4)[k] += nl[k]
+        # (side, mode code, rotations, mixed pass, kernel family) of every
+        # profiled call
+        path = search_plan(d, code, int(batch), 1, tuple(opts) if opts is not None else None, dev)[0]
+        profile.setdefault("calls", []).append((d, code, n, mix is not None, path))
     elif copts is not None:
         _native.check(dev.lib.vesper_search_tuned(*args, copts))
     else:
         _native.check(dev.lib.vesper_search(*args))
     return scores, lin
+
+
+def search_device_sharded(spec, data, vec, mode, ave, rotmats, group=None, probs=None, mix=None, dev=None, **kw):
+    """search_device over every rotation of ``rotmats``; with a
+    torch.distributed process group, this rank searches only its contiguous
+    block of the rotations on its own GPU and the blocks' per-rotation results
+    are gathered in rotation order (shard.search_sharded), so every rank holds
+    what one process would have computed.  Returns device tensors as
+    search_device does."""
+    dev = dev or default_device()
+    if group is None:
+        return search_device(spec, data, vec, mode, ave, rotmats, probs=probs, mix=mix, dev=dev, **kw)
+    from . import shard
+    code = mode if isinstance(mode, int) else MODE_CODES[mode]
+    nscore = dev.lib.vesper_search_nscore(code, 1 if mix is not None else 0)
+
+    def block(lo, hi):
+        if hi <= lo:
+            return np.zeros((0, nscore), np.float32), np.zeros((0, nscore), np.int32)
+        sc, ln = search_device(spec, data, vec, mode, ave, rotmats[lo:hi], probs=probs, mix=mix, dev=dev, **kw)
+        return sc.cpu().numpy(), ln.cpu().numpy()
+
+    sc, ln = shard.search_sharded(block, int(rotmats.shape[0]), group)
+    return dev.to_dev(sc), dev.to_dev(ln)
 
 
 _PLANS = {}
@@ -661,8 +689,10 @@ def _out_folder(folder):
 # ----------------------------------------------------------------------------
 
 def search_map_fft(mrc_target, mrc_search, TopN=10, ang=30, mode="VecProduct", is_eval_mode=False, save_path=".",
-                   showPDB=False, folder=None, dev=None, batch=0, timings=None):
-    """VESPER_1_prob_new.py:568-795 with the rotation loops on the GPU."""
+                   showPDB=False, folder=None, dev=None, batch=0, timings=None, group=None):
+    """VESPER_1_prob_new.py:568-795 with the rotation loops on the GPU.  With a
+    torch.distributed process ``group`` the rotations are split across its
+    ranks (one GPU each) and every rank returns the single-process result."""
     dev = dev or default_device()
     if is_eval_mode:
         print("#For Evaluation Mode")
@@ -686,7 +716,8 @@ def search_map_fft(mrc_target, mrc_search, TopN=10, ang=30, mode="VecProduct", i
     angle_comb = calc_angle_comb(ang)
     mats = rot_matrices_device(angle_comb, dev, key=("grid", float(ang)))
     print("###Start Searching###")
-    scores, lin = search_device(spec, qdata, qvec, mode, mrc_target.ave, mats, batch=batch, dev=dev, tuned=True)
+    scores, lin = search_device_sharded(spec, qdata, qvec, mode, mrc_target.ave, mats, group, batch=batch, dev=dev,
+                                        tuned=True)
     top = topn_device(scores, TopN, dev=dev)
     scale = score_scale(mode, mrc_target)
     raw = scores[:, 0].cpu().numpy()
@@ -721,8 +752,8 @@ def search_map_fft(mrc_target, mrc_search, TopN=10, ang=30, mode="VecProduct", i
         # copied to every position it holds
         uang, uinv = np.unique(refine_ang_arr, axis=0, return_inverse=True)
         rmats = dev.to_dev(rot_matrices(uang))
-        rscores, rlin = search_device(spec, qdata, qvec, mode, mrc_target.ave, rmats, batch=batch, dev=dev,
-                                      tuned=True)
+        rscores, rlin = search_device_sharded(spec, qdata, qvec, mode, mrc_target.ave, rmats, group, batch=batch,
+                                              dev=dev, tuned=True)
         sel_u = dev.to_dev(uinv.reshape(-1).astype(np.int64))
         rscores, rlin = rscores.index_select(0, sel_u), rlin.index_select(0, sel_u)
         rtop = [int(i) for i in topn_device(rscores, TopN, dev=dev).cpu().numpy() if i >= 0]
@@ -764,9 +795,12 @@ def search_map_fft(mrc_target, mrc_search, TopN=10, ang=30, mode="VecProduct", i
 
 def search_map_fft_prob(mrc_P1, mrc_P2, mrc_P3, mrc_P4, mrc_target, mrc_search, mrc_search_p1, mrc_search_p2,
                         mrc_search_p3, mrc_search_p4, ang, alpha=0.0, TopN=10, num_proc=4, vave=-10, vstd=-10,
-                        pave=-10, pstd=-10, showPDB=False, folder=None, dev=None, batch=0):
+                        pave=-10, pstd=-10, showPDB=False, folder=None, dev=None, batch=0, group=None):
     """VESPER_1_prob_new.py:798-1141 with both rotation passes and the
-    refinement on the GPU."""
+    refinement on the GPU.  With a torch.distributed process ``group`` each
+    pass splits the rotations across its ranks; the statistics between the
+    passes are taken over the gathered scores of every rotation, so they equal
+    the single-process values."""
     dev = dev or default_device()
     tdata, tvec = _dev_fields(mrc_target, dev)
     qdata, qvec = _dev_fields(mrc_search, dev)
@@ -783,7 +817,7 @@ def search_map_fft_prob(mrc_P1, mrc_P2, mrc_P3, mrc_P4, mrc_target, mrc_search, 
     if vave >= 0 and vstd >= 0 and pstd >= 0 and pave >= 0:
         pass
     else:
-        s1, _ = search_device(spec, qdata, qvec, "prob", 0.0, mats, probs=qprobs, batch=batch, dev=dev)
+        s1, _ = search_device_sharded(spec, qdata, qvec, "prob", 0.0, mats, group, probs=qprobs, batch=batch, dev=dev)
         s1 = s1.cpu().numpy().astype(np.float64) * rd3
         vstd = np.std(s1[:, 0])
         vave = np.mean(s1[:, 0])
@@ -794,7 +828,8 @@ def search_map_fft_prob(mrc_P1, mrc_P2, mrc_P3, mrc_P4, mrc_target, mrc_search, 
     print("ProbScore Std=", _py(pstd), "ProbScore Ave=", _py(pave))
     print()
     mix = (alpha, vstd, vave, pstd, pave)
-    s2, l2 = search_device(spec, qdata, qvec, "prob", 0.0, mats, probs=qprobs, mix=mix, batch=batch, dev=dev)
+    s2, l2 = search_device_sharded(spec, qdata, qvec, "prob", 0.0, mats, group, probs=qprobs, mix=mix, batch=batch,
+                                   dev=dev)
     top = [int(i) for i in topn_device(s2, TopN, column=2, dev=dev).cpu().numpy() if i >= 0]
     s2h = s2.cpu().numpy()
     l2h = l2.cpu().numpy()
@@ -814,7 +849,8 @@ def search_map_fft_prob(mrc_P1, mrc_P2, mrc_P3, mrc_P4, mrc_target, mrc_search, 
         # depends on it alone once the statistics are fixed), then expanded
         uang, uinv = np.unique(refine_ang_list, axis=0, return_inverse=True)
         rmats = dev.to_dev(rot_matrices(uang))
-        rs, rl = search_device(spec, qdata, qvec, "prob", 0.0, rmats, probs=qprobs, mix=mix, batch=batch, dev=dev)
+        rs, rl = search_device_sharded(spec, qdata, qvec, "prob", 0.0, rmats, group, probs=qprobs, mix=mix,
+                                       batch=batch, dev=dev)
         sel_u = dev.to_dev(uinv.reshape(-1).astype(np.int64))
         rs, rl = rs.index_select(0, sel_u), rl.index_select(0, sel_u)
         rtop = [int(i) for i in topn_device(rs, TopN, column=2, dev=dev).cpu().numpy() if i >= 0]
