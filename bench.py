@@ -69,6 +69,7 @@ WORKLOAD = "prop128_s3_a10"
 METRIC = "map-pair alignments/s: learned-proposal vs exhaustive on GPU at ≥99% top-1 match"
 UNIT = "alignments/s"
 HELD_OUT_SEED0 = 30_000_000     # training used seeds [0, 20000)
+EVAL_SEED0, EVAL_PAIRS = 10_000_000, 200   # held-out recall set
 SUB_STEPS, SUB_WARMUP = 5, 3    # timed / warm-up steps of each sub-configuration
 MODE_NAMES = {"V": "VecProduct", "O": "Overlap", "C": "CC", "P": "PCC", "L": "Laplacian"}
 
@@ -76,7 +77,7 @@ MODE_NAMES = {"V": "VecProduct", "O": "Overlap", "C": "CC", "P": "PCC", "L": "La
 # dominant search kernel (pass A of the register two-step passes), mode V, by
 # grid side, from ncu captures of ``bench.py --case search<d>`` (one launch of
 # k_rpass_a at the search's own batch; profiles/k_rpass_a_side<d>_*.md).
-PASS_A_DRAM_PER_ROT = {30: 4426, 75: 4292364}
+PASS_A_DRAM_PER_ROT = {28: 48521, 30: 3778, 32: 8116, 75: 4281444}
 
 
 def parse():
@@ -502,6 +503,17 @@ def run_gb300(args):
         if exh is not None:
             exh["vs_cpu_baseline"] = round(exh["value"] / cb["value"], 1)
             exh["e2e_vs_cpu_baseline"] = round(exh["e2e"]["value"] / cb["value"], 1)
+    if world == 1 and use_prop and not args.no_exhaustive:
+        # held-out recall of the committed network on a fixed seeded set (the
+        # evaluation seeds, disjoint from training and from the bench pairs)
+        ev, _ = proposal.evaluate(dev, net, list(range(EVAL_SEED0, EVAL_SEED0 + EVAL_PAIRS)),
+                                  vg.rot_matrices_device(vg.calc_angle_comb(p.A), dev, key=("grid", float(p.A))),
+                                  frac=p.proposal_frac, N=p.N, fallback_z=p.proposal_fallback_z)
+        line["recall"] = {"pairs": ev["pairs"], "top1_agreement": ev["top1_agreement"],
+                          "top10_recall": round(ev["topN_recall"], 5), "fallback_rate": ev["fallback_rate"],
+                          "winner_in_subset": ev["winner_in_subset_net"],
+                          "max_score_rel_err_when_agreeing": ev["max_score_rel_err_when_agreeing"],
+                          "seeds": f"{EVAL_SEED0}..{EVAL_SEED0 + EVAL_PAIRS - 1} (held out)"}
     if world == 1 and use_prop and not args.no_configs:
         del flush, al
         torch.cuda.empty_cache()

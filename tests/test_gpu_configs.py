@@ -1,0 +1,371 @@
+"""GPU parity at the benchmarked configurations against the reference's own
+outputs over FULL angle grids (fixtures made by running the unmodified
+reference under stand-in modules: tests/golden/make_golden_configs.py):
+
+* the 200^3 / 100^3 pair at s = 2, A = 10, grid side 75, 24,624 rotations plus
+  the refinement set, in every mode (V, O, C, P, L);
+* the prob-mode pair with four probability channels, grids padded to 64^3,
+  A = 15, both passes (statistics and mixed) plus the refinement set;
+* one pair of the uneven 64-pair batch for every grid side the batch produces
+  (11 ... 44: fused, register-pass and radix-pass sides), A = 15.
+
+The inputs are the same coarse fields the reference searched (stored in the
+fixtures).  Bars:
+
+* every rotation's raw score within 1e-4 of the largest score (DOT, the prob
+  and the mixed scores alike);
+* every rotation's best translation equal to the reference's, or, where it
+  differs, a near-tie: the GPU's translation scores within NEAR_TIE of the
+  maximum in the oracle's own correlation volume of that rotation (the
+  oracle is bit-exact to the reference on these fields), recomputed here for
+  every such rotation;
+* the global and the refined top-10 rotations and translations index-exact;
+  in mode Overlap, whose scores are integer counts computed by float FFTs,
+  equal up to reordering among scores within the score tolerance;
+* the drop-in search_map_fft / search_map_fft_prob print the reference's
+  model lines byte for byte, and its get_score values within 1e-4.
+"""
+import contextlib
+import io
+import os
+import re
+import types
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import vesper_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+SCORE_RTOL = 1e-4
+NEAR_TIE = 1e-5
+
+
+def _vg():
+    from vesper_python_gb300 import vesper as vg
+    return vg
+
+
+def dense(g, prefix):
+    """A field stored sparse in a fixture (flat indices of the non-zero voxels
+    and their values) as a dense array."""
+    shape = tuple(int(v) for v in g[f"{prefix}_shape"])
+    val = g[f"{prefix}_val"]
+    out = np.zeros((int(np.prod(shape[:3])),) + shape[3:], val.dtype)
+    out[g[f"{prefix}_idx"]] = val
+    return out.reshape(shape)
+
+
+@pytest.fixture(scope="module")
+def p200(golden_dir):
+    return dict(np.load(os.path.join(golden_dir, "search_pair200.npz")))
+
+
+@pytest.fixture(scope="module")
+def prob64(golden_dir):
+    return dict(np.load(os.path.join(golden_dir, "prob_pair128_pad64.npz")))
+
+
+@pytest.fixture(scope="module")
+def unev(golden_dir):
+    return dict(np.load(os.path.join(golden_dir, "uneven_sides.npz")))
+
+
+def _lin(trans, d):
+    t = np.asarray(trans).astype(np.int64)
+    return (t[:, 0] * d + t[:, 1]) * d + t[:, 2]
+
+
+def _workers():
+    return os.cpu_count() or 1
+
+
+def near_tie_gaps(vol_fn, rows, gpu_lin):
+    """For each rotation row r: (max(vol) - vol[gpu_lin[r]]) / max|vol| in the
+    oracle's own volume vol = vol_fn(r)."""
+    gaps = []
+    for r in rows:
+        flat = np.asarray(vol_fn(r), np.float64).reshape(-1)
+        gaps.append((flat.max() - flat[gpu_lin[r]]) / max(np.max(np.abs(flat)), 1e-300))
+    return np.array(gaps)
+
+
+def check_rotations(what, sc, ln, ref_sc, ref_trans, d, vol_fn):
+    """Scores within SCORE_RTOL of the largest; every differing translation a
+    near-tie in the oracle's volume.  Returns the number of near-ties."""
+    scale = np.max(np.abs(ref_sc))
+    err = np.max(np.abs(sc - ref_sc)) / scale
+    assert err < SCORE_RTOL, f"{what}: score error {err:.3g}"
+    lin_ref = _lin(ref_trans, d)
+    mism = np.nonzero(ln != lin_ref)[0]
+    if len(mism):
+        gaps = near_tie_gaps(vol_fn, mism, ln)
+        bad = mism[gaps > NEAR_TIE]
+        assert len(bad) == 0, f"{what}: rotations {bad[:10].tolist()} are not near-ties (gaps {gaps.max():.3g})"
+    return len(mism)
+
+
+def check_topn(what, top_g, top_r, ln, lin_ref, ref_sc, exact):
+    """Top-N index-exact (rotations and translations); with exact=False,
+    equal up to reordering among scores within the tolerance."""
+    tol = SCORE_RTOL * np.max(np.abs(ref_sc))
+    if exact:
+        assert np.array_equal(top_g, top_r), f"{what}: top-N {top_g.tolist()} != {top_r.tolist()}"
+    else:
+        assert len(set(top_g.tolist())) == len(top_g)
+        assert np.all(np.abs(ref_sc[top_g] - ref_sc[top_r]) <= tol), what
+        cut = ref_sc[top_r[-1]]
+        for r in set(top_g.tolist()) ^ set(top_r.tolist()):
+            assert abs(ref_sc[r] - cut) <= tol, what
+    same = np.isin(top_g, top_r)
+    assert np.array_equal(ln[top_g][same], lin_ref[top_g][same]), f"{what}: top-N translations differ"
+
+
+def _topn(dev, sc, n, column=0):
+    vg = _vg()
+    t = torch.as_tensor(np.ascontiguousarray(sc, np.float32)).to(dev.device)
+    if t.dim() == 1:
+        t = t.reshape(-1, 1)
+    return vg.topn_device(t, n, column=column, dev=dev).cpu().numpy()
+
+
+def _maps(g, pre=""):
+    """Target / query map objects with the fields search_map_fft reads."""
+    d = int(g[pre + "dim"])
+    s1, s2 = g[pre + "stats1"], g[pre + "stats2"]
+    t = types.SimpleNamespace(data=dense(g, pre + "data1"), vec=dense(g, pre + "vec1"), xdim=d, ydim=d, zdim=d,
+                              cent=g[pre + "cent1"], orig=g[pre + "orig1"], xwidth=float(g[pre + "xwidth2"]),
+                              dsum=s1[0], Nact=s1[1], ave=s1[2], std=s1[3], std_norm_ave=s1[4])
+    q = types.SimpleNamespace(data=dense(g, pre + "data2"), vec=dense(g, pre + "vec2"), xdim=d, ydim=d, zdim=d,
+                              cent=g[pre + "cent2"], orig=g[pre + "orig2"], xwidth=float(g[pre + "xwidth2"]),
+                              dsum=s2[0], Nact=s2[1], ave=s2[2], std=s2[3], std_norm_ave=s2[4])
+    return t, q
+
+
+def _model_lines(text, prefix):
+    return [ln for ln in text.splitlines() if re.match(rf"^{re.escape(prefix)}\d+ Rotation=", ln)]
+
+
+def _nums(text, key):
+    return [float(re.search(rf"{key}\s*([-0-9.e+]+)", ln).group(1)) for ln in text.splitlines() if key in ln]
+
+
+def _search_scalar(dev, g, pre, mode, angles, opts=None):
+    """GPU search of one mode over ``angles`` on a fixture's fields: raw
+    scores (float64) and linear translations (``opts``: a kernel family
+    forced, else the tuned automatic choice)."""
+    vg = _vg()
+    t, q = _maps(g, pre)
+    name = orc.MODES[mode]
+    spec = vg.target_spectra_device(dev.to_dev(t.data), dev.to_dev(t.vec), name, t.ave, dev=dev)
+    sc, ln = vg.search_device(spec, dev.to_dev(q.data), dev.to_dev(q.vec), name, t.ave,
+                              dev.to_dev(vg.rot_matrices(angles)), dev=dev, tuned=opts is None, opts=opts)
+    return sc[:, 0].cpu().numpy().astype(np.float64), ln[:, 0].cpu().numpy()
+
+
+def _scalar_vol_fn(g, pre, mode, angles):
+    t, q = _maps(g, pre)
+    ts = orc.target_spectra(orc.mode_field(mode, t.data, t.vec, t.ave))
+
+    def vol(r):
+        nv, nd = orc.rot_mrc(q.data, q.vec, angles[r])
+        return sum(orc.correlate(ts, orc.mode_field(mode, nd, nv, t.ave), workers=_workers()))
+    return vol
+
+
+def _check_scalar_search(dev, g, pre, mode, what, opts=None):
+    """Global grid and refinement set of one scalar-mode search against the
+    reference's recorded calls; top-N of both.  Keys: ``<mode>_score`` ... in
+    the pair200 fixture (pre = ""), ``d<side>_score`` ... in the uneven one."""
+    key = (lambda name: f"{mode}_{name}") if pre == "" else (lambda name: pre + name)
+    t, _ = _maps(g, pre)
+    d = int(g[pre + "dim"])
+    A = 10.0 if pre == "" else 15.0
+    scale = orc.score_scale(mode, t.std, t.std_norm_ave)
+    out = {}
+    for part, angles, rsc, rtr in (
+            ("global", orc.calc_angle_comb(A), g[key("score")], g[key("trans")]),
+            ("refine", g[key("refine_angles")], g[key("refine_score")], g[key("refine_trans")])):
+        ref = np.asarray(rsc, np.float64) / scale
+        sc, ln = _search_scalar(dev, g, pre, mode, angles, opts)
+        n_tie = check_rotations(f"{what} {part}", sc, ln, ref, rtr, d, _scalar_vol_fn(g, pre, mode, angles))
+        top_g = _topn(dev, sc, 10)
+        top_r = orc.topn(ref, 10)
+        check_topn(f"{what} {part}", top_g, top_r, ln, _lin(rtr, d), ref, exact=(mode != "O"))
+        out[part] = n_tie
+    # the refined list: the refinement set's top-10 rows, as the reference kept them
+    assert np.array_equal(np.asarray(g[key("refine_angles")])[orc.topn(
+        np.asarray(g[key("refine_score")], np.float64) / scale, 10)], g[key("refined_angle")])
+    return out
+
+
+# ---------------------------------------------------------------------------
+# configuration 1: 200^3 / 100^3 pair, side 75, every mode
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_pair200_full_grid_and_refinement_vs_reference(dev, p200, mode):
+    assert int(p200["dim"]) == 75
+    ties = _check_scalar_search(dev, p200, "", mode, f"pair200 {mode}")
+    print(f"pair200 {mode}: near-ties {ties}")
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_pair200_drop_in_search_prints_reference_models(dev, p200, golden_dir, mode):
+    """search_map_fft on the fixture's fields: the M (global top-10) and #
+    (refined models) lines byte for byte, get_score values within 1e-4."""
+    vg = _vg()
+    t, q = _maps(p200, "")
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        vg.search_map_fft(t, q, TopN=10, ang=10.0, mode=orc.MODES[mode], dev=dev)
+    out = buf.getvalue()
+    ref = open(os.path.join(golden_dir, f"search_pair200_{mode}.txt")).read()
+    for prefix in ("M", "#"):
+        got, want = _model_lines(out, prefix), _model_lines(ref, prefix)
+        assert len(want) == 10
+        if mode == "O":   # integer scores: allow reordering among exact ties (see check_topn)
+            assert sorted(got) == sorted(want), prefix
+        else:
+            assert got == want, prefix
+    for key in ("Score=", "CC=", "PCC=", "Overlap="):
+        o, r = _nums(out, key), _nums(ref, key)
+        assert len(o) == len(r) == 10
+        if mode == "O":
+            o, r = sorted(o), sorted(r)
+        assert np.allclose(o, r, rtol=1e-4, atol=1e-6), key
+
+
+# ---------------------------------------------------------------------------
+# configuration 3: prob mode, grids padded to 64^3
+# ---------------------------------------------------------------------------
+def _prob_setup(dev, g):
+    vg = _vg()
+    d = int(g["dim"])
+    tdata, tvec, tprobs = dense(g, "data1"), dense(g, "vec1"), np.moveaxis(dense(g, "probs1"), 3, 0).copy()
+    qdata, qvec, qprobs = dense(g, "data2"), dense(g, "vec2"), np.moveaxis(dense(g, "probs2"), 3, 0).copy()
+    spec = vg.target_spectra_device(dev.to_dev(tdata.astype(np.float64)), dev.to_dev(tvec), "prob", 0.0,
+                                    probs=dev.to_dev(tprobs), dev=dev)
+    tspec = orc.target_spectra([tvec[..., 0], tvec[..., 1], tvec[..., 2]] + list(tprobs))
+    return d, spec, tspec, (tdata, tvec, tprobs), (qdata, qvec, qprobs)
+
+
+def test_prob64_both_passes_and_refinement_vs_reference(dev, prob64):
+    vg = _vg()
+    g = prob64
+    d, spec, tspec, _, (qdata, qvec, qprobs) = _prob_setup(dev, g)
+    assert d == 64
+    rd3 = 1.0 / d ** 3
+    angles = orc.calc_angle_comb(15.0)
+    qd, qv, qp = dev.to_dev(qdata.astype(np.float64)), dev.to_dev(qvec), dev.to_dev(qprobs)
+    mats = dev.to_dev(vg.rot_matrices(angles))
+    s1, l1 = vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, dev=dev, tuned=True)
+    s1, l1 = s1.cpu().numpy().astype(np.float64), l1.cpu().numpy()
+
+    def vols(r, ang, kind, st=None):
+        res = orc.rot_mrc_prob(qdata, qvec, *qprobs, ang[r])
+        nv = res[0]
+        cv = orc.correlate(tspec[:3], [nv[..., 0], nv[..., 1], nv[..., 2]], workers=_workers())
+        cp = orc.correlate(tspec[3:], list(res[2:6]), workers=_workers())
+        if kind == "v":
+            return sum(cv)
+        if kind == "p":
+            return sum(cp)
+        vstd, vave, pstd, pave = st
+        sv = (sum(cv) - np.float32(vave)) / np.float32(vstd)
+        sp = (sum(cp) - np.float32(pave)) / np.float32(pstd)
+        return np.float32(0.5) * sv + np.float32(0.5) * sp
+
+    check_rotations("prob pass 1 vec", s1[:, 0], l1[:, 0], g["pass1_vscore"], g["pass1_vtrans"], d,
+                    lambda r: vols(r, angles, "v"))
+    check_rotations("prob pass 1 prob", s1[:, 1], l1[:, 1], g["pass1_pscore"], g["pass1_ptrans"], d,
+                    lambda r: vols(r, angles, "p"))
+    # the statistics of the reference's own pass-1 scores, then the mixed pass
+    st = orc.prob_stats(g["pass1_vscore"], g["pass1_pscore"], rd3)
+    mine = orc.prob_stats(s1[:, 0], s1[:, 1], rd3)
+    assert np.allclose(mine, st, rtol=1e-5)
+    mix = (0.5,) + tuple(st)
+    s2, l2 = vg.search_device(spec, qd, qv, "prob", 0.0, mats, probs=qp, mix=mix, dev=dev, tuned=True)
+    s2, l2 = s2.cpu().numpy().astype(np.float64), l2.cpu().numpy()
+    check_rotations("prob pass 2 mixed", s2[:, 2], l2[:, 2], g["pass2_mscore"], g["pass2_mtrans"], d,
+                    lambda r: vols(r, angles, "m", st))
+    top_g = _topn(dev, s2[:, 2], 10)
+    top_r = orc.topn(g["pass2_mscore"], 10)
+    check_topn("prob global", top_g, top_r, l2[:, 2], _lin(g["pass2_mtrans"], d), g["pass2_mscore"], exact=True)
+    # refinement: the reference's refinement list around the same top-10
+    ref_angles = g["refine_angles"]
+    assert np.array_equal(ref_angles, orc.refine_angles(angles[top_r]))
+    rs, rl = vg.search_device(spec, qd, qv, "prob", 0.0, dev.to_dev(vg.rot_matrices(ref_angles)), probs=qp,
+                              mix=mix, dev=dev, tuned=True)
+    rs, rl = rs.cpu().numpy().astype(np.float64), rl.cpu().numpy()
+    check_rotations("prob refine mixed", rs[:, 2], rl[:, 2], g["refine_mscore"], g["refine_mtrans"], d,
+                    lambda r: vols(r, ref_angles, "m", st))
+    rtop_g = _topn(dev, rs[:, 2], 10)
+    rtop_r = orc.topn(g["refine_mscore"], 10)
+    check_topn("prob refine", rtop_g, rtop_r, rl[:, 2], _lin(g["refine_mtrans"], d), g["refine_mscore"], exact=True)
+    assert np.array_equal(ref_angles[rtop_g], g["refined_angle"])
+    assert np.array_equal(np.stack([_lin(g["refined_mtrans"], d)]), np.stack([rl[rtop_g, 2]]))
+
+
+def test_prob64_drop_in_search_prints_reference_models(dev, prob64, golden_dir):
+    """search_map_fft_prob on the fixture's fields: the refined models' lines
+    byte for byte."""
+    vg = _vg()
+    g = prob64
+    d = int(g["dim"])
+    tdata, tvec, tprobs = dense(g, "data1"), dense(g, "vec1"), dense(g, "probs1")
+    qdata, qvec, qprobs = dense(g, "data2"), dense(g, "vec2"), dense(g, "probs2")
+    pos = tdata[tdata > 0].astype(np.float64)
+    t = types.SimpleNamespace(data=tdata, vec=tvec, xdim=d, cent=g["cent1"], orig=np.zeros(3),
+                              xwidth=float(g["xwidth2"]), ave=np.mean(pos), std=np.linalg.norm(pos),
+                              std_norm_ave=np.linalg.norm(pos - np.mean(pos)))
+    q = types.SimpleNamespace(data=qdata, vec=qvec, xdim=d, cent=g["cent2"], xwidth=float(g["xwidth2"]))
+    P = [types.SimpleNamespace(data=tprobs[..., c]) for c in range(4)]
+    Q = [types.SimpleNamespace(data=qprobs[..., c]) for c in range(4)]
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        vg.search_map_fft_prob(*P, t, q, *Q, ang=15.0, alpha=0.5, TopN=10, dev=dev)
+    out = buf.getvalue()
+    ref = open(os.path.join(golden_dir, "prob_pair128_pad64.txt")).read()
+    assert len(_model_lines(ref, "#")) == 10
+    assert _model_lines(out, "#") == _model_lines(ref, "#")
+    got = [ln for ln in out.splitlines() if ln.startswith("Translation=")]
+    want = [ln for ln in ref.splitlines() if ln.startswith("Translation=")]
+    assert [ln.split(" Probability Score=")[0] for ln in got] == [ln.split(" Probability Score=")[0] for ln in want]
+
+
+# ---------------------------------------------------------------------------
+# configuration 2: every grid side of the uneven batch
+# ---------------------------------------------------------------------------
+def test_uneven_sides_full_grid_and_refinement_vs_reference(dev, unev):
+    vg = _vg()
+    sides = [int(s) for s in unev["sides"]]
+    assert sides[0] <= 12 and sides[-1] >= 44 and 18 in sides and 22 in sides
+    paths = {}
+    for d in sides:
+        pre = f"d{d}_"
+        assert int(unev[pre + "dim"]) == d
+        paths[d] = vg.search_plan(d, "VecProduct", dev=dev)[0]
+        _check_scalar_search(dev, unev, pre, "V", f"uneven side {d}")
+    # the automatic choice covers the fused kernel and the register passes;
+    # the radix-stage passes are held to the same bars on three of the sides
+    assert set(paths.values()) == {1, 2}, paths
+    for d in (18, 27, 44):
+        _check_scalar_search(dev, unev, f"d{d}_", "V", f"uneven side {d} radix passes", opts=(0, 0, 0))
+
+
+def test_uneven_sides_drop_in_search_prints_reference_models(dev, unev):
+    vg = _vg()
+    for d in [int(s) for s in unev["sides"]]:
+        pre = f"d{d}_"
+        t, q = _maps(unev, pre)
+        buf = io.StringIO()
+        with contextlib.redirect_stdout(buf):
+            vg.search_map_fft(t, q, TopN=10, ang=15.0, mode="VecProduct", dev=dev)
+        out = buf.getvalue()
+        ref = str(unev[pre + "stdout"])
+        for prefix in ("M", "#"):
+            assert _model_lines(out, prefix) == _model_lines(ref, prefix), (d, prefix)
+        for key in ("Score=", "CC=", "PCC=", "Overlap="):
+            assert np.allclose(_nums(out, key), _nums(ref, key), rtol=1e-4, atol=1e-6), (d, key)

@@ -3,7 +3,8 @@
 For a (grid side, mode) pair it times vesper_search_tuned over a sample of
 rotations for every candidate of
 
-  batch      rotations per pipeline step (8 to 2048, S + U of a step <= 96 MB)
+  batch      rotations per pipeline step (8 to 128, and up to 2048 while S + U of
+             a step stay within 160 MB)
   cchunk     channels gathered and transformed per pass-A block
   W          spectrum columns per pass-B block
 
@@ -68,14 +69,14 @@ def _save_disk(entries):
 
 
 BATCHES = (8, 16, 32, 64, 128, 256, 512, 1024, 2048)
-BATCH_BYTES = 96 << 20      # S + U of one batch, kept near the L2 size
+BATCH_BYTES = 160 << 20     # S + U of one batch above 128 rotations: about the L2 size
 
 
 def candidates(nch, dim=None, ngrp=1):
     per = None if dim is None else (nch + ngrp) * dim * dim * (dim // 2 + 1) * 8
     out = []
     for batch in BATCHES:
-        if batch > 64 and (per is None or batch * per > BATCH_BYTES):
+        if batch > 128 and (per is None or batch * per > BATCH_BYTES):
             continue
         for cc in sorted({1, nch}):
             for W in (16, 32):

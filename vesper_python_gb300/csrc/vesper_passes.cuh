@@ -85,6 +85,17 @@ __device__ __forceinline__ void sample_a(const PassA2 &a, const float (&F)[9], i
     sample_fast<MODE>(a.src, F, x, y, z, out);
 }
 
+// sample_a for a side known at compile time (sample_ct in modes V/O/C/P).
+template <int MODE, int NCH, int D>
+__device__ __forceinline__ void sample_a_ct(const PassA2 &a, const float (&F)[9], int b, int x, int y, int z,
+                                            float *out) {
+    if constexpr (MODE == VESPER_MODE_VEC || MODE == VESPER_MODE_OVERLAP || MODE == VESPER_MODE_CC ||
+                  MODE == VESPER_MODE_PCC)
+        sample_ct<MODE, D>(a.src, F, x, y, z, out);
+    else
+        sample_a<MODE, NCH>(a, F, b, x, y, z, out);
+}
+
 __host__ __device__ inline size_t smem_a2(int d, int ntab, int cchunk) {
     const PlaneGeom g = plane_geom(d);
     return smem_head(d, ntab) + align16(16 * sizeof(float)) +

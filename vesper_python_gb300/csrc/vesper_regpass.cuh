@@ -27,6 +27,62 @@ struct RGeom {
     static constexpr int Hp = H | 1;
 };
 
+// Gather of the packed rows (2p, 2p+1) of NIT items, GI items per thread in
+// flight: every item's source indices first, then all their loads, then the
+// values (V/O/C/P modes; the rare multi-candidate voxels of odd sides take the
+// general gather).  map(item, pl, p, z) gives an item's plane slot, packed
+// line and z (false: skip); store(pl, p, z, v0, v1) writes its values.
+template <int MODE, int NCH, int D, int GI, class Map, class Store>
+__device__ __forceinline__ void gather_rows_batched(const PassA2 &a, const float (&Fr)[9], int b, int x0, int NIT,
+                                                    Map map, Store store) {
+    const int T = blockDim.x;
+    for (int base = threadIdx.x; base < NIT; base += GI * T) {
+        int src[GI][2], pl[GI], pp[GI], zz[GI];
+        bool on[GI];
+#pragma unroll
+        for (int g = 0; g < GI; ++g) {
+            const int item = base + g * T;
+            on[g] = item < NIT && map(item, pl[g], pp[g], zz[g]);
+            src[g][0] = src[g][1] = -1;
+            if (on[g]) {
+                const int x = x0 + pl[g], y0 = 2 * pp[g];
+                src[g][0] = gather_index_fast(Fr, D, x, y0, zz[g]);
+                if (y0 + 1 < D) src[g][1] = gather_index_fast(Fr, D, x, y0 + 1, zz[g]);
+            }
+        }
+        float4 q[GI][2];
+#pragma unroll
+        for (int g = 0; g < GI; ++g)
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                q[g][h] = src[g][h] >= 0 ? __ldg(a.src.q4 + src[g][h]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int g = 0; g < GI; ++g) {
+            if (!on[g]) continue;
+            float v[2][NCH];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int y = 2 * pp[g] + h;
+                if (src[g][h] == -2) {
+                    sample<MODE>(a.src, Fr, x0 + pl[g], y, zz[g], v[h]);
+                } else {
+                    const float4 w = q[g][h];
+                    const bool hit = src[g][h] >= 0 && w.w != 0.f;
+                    if (MODE == VESPER_MODE_VEC) {
+                        float r3[3] = {0.f, 0.f, 0.f};
+                        if (hit) rotate_vec(Fr, w.x, w.y, w.z, r3);
+#pragma unroll
+                        for (int c = 0; c < NCH; ++c) v[h][c] = r3[c < 3 ? c : 0];
+                    } else {
+                        v[h][0] = hit ? w.x : 0.f;
+                    }
+                }
+            }
+            store(pl[g], pp[g], zz[g], v[0], v[1]);
+        }
+    }
+}
+
 // Pass A keeps, per channel, a plane of 2*NP rows of Hp complex values: packed
 // z line p lives in the storage of rows 2p and 2p+1 (D <= 2 Hp elements) and is
 // unpacked into exactly those two rows.
@@ -76,9 +132,30 @@ __global__ void __launch_bounds__(256, rpass_a_ctas<MODE, N1, N2>()) k_rpass_a(c
     for (int i = 0; i < 9; ++i) Fr[i] = F[i];
     for (int c0 = 0; c0 < NCH; c0 += a.cchunk) {
         const int cn = min(a.cchunk, NCH - c0);
-        // gather rows (2p, 2p+1) into packed z line p (natural z order)
-        for (Walk2 w(D); w.o < NP; w.next()) {
-            const int p = w.o, z = w.i, y0 = 2 * p;
+        // gather rows (2p, 2p+1) into packed z line p (natural z order): each
+        // warp covers a tile of 4 packed lines x 8 z (8 rows x 8 z voxels, so
+        // its source voxels cluster in fewer cache lines than a row of 32 z)
+        constexpr int TP = (NP + 3) / 4, TZ = (D + 7) / 8;
+        if constexpr (MODE == VESPER_MODE_VEC || MODE == VESPER_MODE_OVERLAP || MODE == VESPER_MODE_CC ||
+                      MODE == VESPER_MODE_PCC) {
+            auto map = [&](int item, int &pl, int &p, int &z) {
+                const int lane = item & 31, tile = item >> 5;
+                pl = 0;
+                p = (tile / TZ) * 4 + (lane >> 3);
+                z = (tile % TZ) * 8 + (lane & 7);
+                return p < NP && z < D;
+            };
+            auto store = [&](int, int p, int z, const float *v0, const float *v1) {
+#pragma unroll
+                for (int c = 0; c < NCH; ++c)
+                    if (c >= c0 && c < c0 + cn) plane[(c - c0) * PS + 2 * p * Hp + z] = make_float2(v0[c], v1[c]);
+            };
+            gather_rows_batched<MODE, NCH, D, 2>(a, Fr, b, x, TP * TZ * 32, map, store);
+        } else
+        for (int t = threadIdx.x; t < TP * TZ * 32; t += blockDim.x) {
+            const int lane = t & 31, tile = t >> 5;
+            const int p = (tile / TZ) * 4 + (lane >> 3), z = (tile % TZ) * 8 + (lane & 7), y0 = 2 * p;
+            if (p >= NP || z >= D) continue;
             float v0[NCH], v1[NCH];
             sample_a<MODE, NCH>(a, Fr, b, x, y0, z, v0);
             if (y0 + 1 < D) {
@@ -183,6 +260,93 @@ __global__ void __launch_bounds__(256, rpass_a_ctas<MODE, N1, N2>()) k_rpass_a(c
 }
 
 // ---------------------------------------------------------------------------
+// Pass A for sides up to 32 with whole lines in registers: PL x-planes per
+// CTA; one packed z line per thread (DFT + unpack in registers), then one y
+// column per thread (DFT in registers, straight to S).
+constexpr int kLinePlanes = 2;   // x-planes per CTA of the whole-line passes
+
+template <int D>
+struct LineGeom {
+    static constexpr int H = D / 2 + 1, NP = (D + 1) / 2, Hp = H | 1;
+    static constexpr int LS = 2 * Hp + 1;   // packed-line stride (odd)
+    static constexpr int PS = NP * LS;      // plane stride per channel
+};
+template <int D, int NCH, int PL>
+__host__ __device__ inline size_t smem_ra_line() {
+    return 64 + (size_t)PL * NCH * LineGeom<D>::PS * sizeof(float2);
+}
+
+template <int MODE, int NCH, int N1, int N2, int PL>
+__global__ void __launch_bounds__(256, 2) k_rpass_a_line(const PassA2 a) {
+    constexpr int D = N1 * N2;
+    using L = LineGeom<D>;
+    constexpr int H = L::H, NP = L::NP, Hp = L::Hp, LS = L::LS, PS = L::PS;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float *F = (float *)smem;
+    float2 *buf = (float2 *)(smem + 64);   // [PL][NCH][NP][LS]
+    const int x0 = blockIdx.x * PL, b = blockIdx.y, r = a.r0 + b;
+    if (threadIdx.x < 9) F[threadIdx.x] = a.rotmats[(size_t)r * 9 + threadIdx.x];
+    if (x0 == 0 && threadIdx.x < a.nscore) a.keys[(size_t)r * a.nscore + threadIdx.x] = 0ull;
+    __syncthreads();
+    float Fr[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fr[i] = F[i];
+    // gather: each warp covers a tile of 4 packed lines x 8 z of one plane
+    constexpr int TP = (NP + 3) / 4, TZ = (D + 7) / 8;
+    for (int t = threadIdx.x; t < PL * TP * TZ * 32; t += blockDim.x) {
+        const int lane = t & 31, tile = t >> 5;
+        const int pl = tile / (TP * TZ), tt = tile % (TP * TZ);
+        const int p = (tt / TZ) * 4 + (lane >> 3), z = (tt % TZ) * 8 + (lane & 7), y0 = 2 * p;
+        const int x = x0 + pl;
+        if (p >= NP || z >= D || x >= D) continue;
+        float v0[NCH], v1[NCH];
+        sample_a_ct<MODE, NCH, D>(a, Fr, b, x, y0, z, v0);
+        if (y0 + 1 < D) {
+            sample_a_ct<MODE, NCH, D>(a, Fr, b, x, y0 + 1, z, v1);
+        } else {
+#pragma unroll
+            for (int c = 0; c < NCH; ++c) v1[c] = 0.f;
+        }
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) buf[(pl * NCH + c) * PS + p * LS + z] = make_float2(v0[c], v1[c]);
+    }
+    __syncthreads();
+    // z: one packed line per thread; DFT and unpack into rows 2p (offset 0)
+    // and 2p + 1 (offset Hp) of the line's own storage
+    for (int t = threadIdx.x; t < PL * NCH * NP; t += blockDim.x) {
+        const int p = t % NP, pc = t / NP;
+        if (x0 + pc / NCH >= D) continue;
+        float2 *line = buf + pc * PS + p * LS;
+        float2 v[D];
+#pragma unroll
+        for (int j = 0; j < D; ++j) v[j] = line[j];
+        rdft<D, false>(v);
+        const bool two = 2 * p + 1 < D;
+#pragma unroll
+        for (int k = 0; k < H; ++k) {
+            float2 A, B;
+            unpack_pair(v[k], v[(D - k) % D], A, B);
+            line[k] = A;
+            line[Hp + k] = two ? B : make_float2(0.f, 0.f);
+        }
+    }
+    __syncthreads();
+    // y: one column (plane, channel, kz) per thread -> S rows ky
+    for (int t = threadIdx.x; t < PL * NCH * H; t += blockDim.x) {
+        const int kz = t % H, pc = t / H, pl = pc / NCH, c = pc % NCH, x = x0 + pl;
+        if (x >= D) continue;
+        const float2 *pln = buf + pc * PS + kz;
+        float2 v[D];
+#pragma unroll
+        for (int y = 0; y < D; ++y) v[y] = pln[(y >> 1) * LS + (y & 1) * Hp];
+        rdft<D, false>(v);
+        float2 *dst = a.S + (((size_t)b * NCH + c) * D + x) * (size_t)D * H + kz;
+#pragma unroll
+        for (int ky = 0; ky < D; ++ky) dst[(size_t)ky * H] = v[ky];
+    }
+}
+
+// ---------------------------------------------------------------------------
 template <int NCH, int NGRP, int N1, int N2>
 __global__ void __launch_bounds__(256) k_rpass_b(const PassB2 a) {
     using G = RGeom<N1, N2>;
@@ -255,6 +419,38 @@ __global__ void __launch_bounds__(256) k_rpass_b(const PassB2 a) {
 #pragma unroll
             for (int j1 = 0; j1 < N1; ++j1) dst[((size_t)g * D + j2 + N2 * j1) * dH + j] = v[j1];
     }
+}
+
+// ---------------------------------------------------------------------------
+// Pass B for sides up to 32 with one score group: one spectrum column j =
+// ky H + kz per thread, whole x lines in registers -- for every channel the
+// forward x DFT of its S column, times conj(T) added into the column's sum,
+// then the inverse x DFT of the sum straight to U.  No shared memory.
+constexpr int kLineBThreads = 128;
+
+template <int NCH, int N1, int N2>
+__global__ void __launch_bounds__(kLineBThreads) k_rpass_b_line(const PassB2 a) {
+    constexpr int D = N1 * N2, H = D / 2 + 1, dH = D * H;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (j >= dH) return;
+    const float2 *src = a.S + (size_t)b * NCH * D * dH + j;
+    float2 acc[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) acc[k] = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int c = 0; c < NCH; ++c) {
+        float2 v[D];
+#pragma unroll
+        for (int x = 0; x < D; ++x) v[x] = src[(size_t)(c * D + x) * dH];
+        rdft<D, false>(v);
+        const float2 *T = a.T + (size_t)c * D * dH + j;
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[k] = cadd(acc[k], cmul(T[(size_t)k * dH], v[k]));
+    }
+    rdft<D, true>(acc);
+    float2 *dst = a.U + (size_t)b * D * dH + j;
+#pragma unroll
+    for (int x = 0; x < D; ++x) dst[(size_t)x * dH] = acc[x];
 }
 
 // ---------------------------------------------------------------------------
@@ -392,12 +588,26 @@ struct RegEntry {
 template <int MODE, int NCH, int NGRP, int N1, int N2>
 struct RegPath {
     static void a(dim3 g, int T, size_t s, cudaStream_t st, const PassA2 &p) {
-        allow_smem(k_rpass_a<MODE, NCH, N1, N2>, s);
-        k_rpass_a<MODE, NCH, N1, N2><<<g, T, s, st>>>(p);
+        if constexpr (N1 * N2 <= 32 && MODE != VESPER_MODE_LAPLACIAN) {
+            // whole lines in registers, kLinePlanes x-planes per CTA
+            constexpr int PL = kLinePlanes;
+            const size_t sl = smem_ra_line<N1 * N2, NCH, PL>();
+            allow_smem(k_rpass_a_line<MODE, NCH, N1, N2, PL>, sl);
+            k_rpass_a_line<MODE, NCH, N1, N2, PL><<<dim3((N1 * N2 + PL - 1) / PL, g.y), 256, sl, st>>>(p);
+        } else {
+            allow_smem(k_rpass_a<MODE, NCH, N1, N2>, s);
+            k_rpass_a<MODE, NCH, N1, N2><<<g, T, s, st>>>(p);
+        }
     }
     static void b(dim3 g, int T, size_t s, cudaStream_t st, const PassB2 &p) {
-        allow_smem(k_rpass_b<NCH, NGRP, N1, N2>, s);
-        k_rpass_b<NCH, NGRP, N1, N2><<<g, T, s, st>>>(p);
+        if constexpr (N1 * N2 <= 32 && NGRP == 1) {
+            constexpr int dH = N1 * N2 * (N1 * N2 / 2 + 1);
+            k_rpass_b_line<NCH, N1, N2><<<dim3((dH + kLineBThreads - 1) / kLineBThreads, g.y), kLineBThreads, 0,
+                                          st>>>(p);
+        } else {
+            allow_smem(k_rpass_b<NCH, NGRP, N1, N2>, s);
+            k_rpass_b<NCH, NGRP, N1, N2><<<g, T, s, st>>>(p);
+        }
     }
     static void c(dim3 g, int T, size_t s, cudaStream_t st, const PassC2 &p, int nscore) {
         if constexpr (NGRP == 1) {

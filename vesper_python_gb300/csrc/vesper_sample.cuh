@@ -111,14 +111,64 @@ __device__ __forceinline__ int gather4_fast(const float (&F)[9], int d, int x, i
     int ox, oy, oz;
     if (!old_index(F, d, hc, (float)ix - hc, (float)iy - hc, (float)iz - hc, ox, oy, oz)) return -1;
     const int i = (ox * d + oy) * d + oz;
-    const float4 v = q4[i];
+    const float4 v = __ldg(q4 + i);   // read-only path: the query is not written during a search
     if (v.w == 0.f) return -1;
     out = v;
     return i;
 }
 
+// Source index of destination (x, y, z) when every axis has one candidate
+// row (the common case): the voxel (its mask not yet read), -1 for none (out
+// of bounds, or no row lands there), -2 when an axis has two candidate rows
+// (odd d, middle index) and the general enumeration of gather4 decides.
+__device__ __forceinline__ int gather_index_fast(const float (&F)[9], int d, int x, int y, int z) {
+    const int ix = cand1(x, d), iy = cand1(y, d), iz = cand1(z, d);
+    if ((ix | iy | iz) < 0) return (ix == -1 || iy == -1 || iz == -1) ? -1 : -2;
+    const float hc = 0.5f * (float)d;
+    int ox, oy, oz;
+    if (!old_index(F, d, hc, (float)ix - hc, (float)iy - hc, (float)iz - hc, ox, oy, oz)) return -1;
+    return (ox * d + oy) * d + oz;
+}
+
 template <int MODE>
 __device__ __forceinline__ void sample(const Src &s, const float *F, int x, int y, int z, float *out);
+
+// sample_fast for a side D known at compile time (modes V, O, C, P): the
+// candidate rows, the bounds and the index arithmetic fold to constants; the
+// rare multi-candidate voxels of odd sides take the general gather.  Same
+// results as sample().
+template <int MODE, int D>
+__device__ __forceinline__ void sample_ct(const Src &s, const float (&F)[9], int x, int y, int z, float *out) {
+    static_assert(MODE == VESPER_MODE_VEC || MODE == VESPER_MODE_OVERLAP || MODE == VESPER_MODE_CC ||
+                  MODE == VESPER_MODE_PCC, "sample_ct: modes V, O, C, P");
+    const int ix = cand1(x, D), iy = cand1(y, D), iz = cand1(z, D);
+    bool hit = false;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((ix | iy | iz) < 0) {
+        if (ix == -2 || iy == -2 || iz == -2) {
+            if (ix != -1 && iy != -1 && iz != -1) {
+                sample<MODE>(s, F, x, y, z, out);
+                return;
+            }
+        }
+    } else {
+        constexpr float hc = 0.5f * (float)D;
+        int ox, oy, oz;
+        if (old_index(F, D, hc, (float)ix - hc, (float)iy - hc, (float)iz - hc, ox, oy, oz)) {
+            v = __ldg(s.q4 + (ox * D + oy) * D + oz);
+            hit = v.w != 0.f;
+        }
+    }
+    if (MODE == VESPER_MODE_VEC) {
+        float r[3] = {0.f, 0.f, 0.f};
+        if (hit) rotate_vec(F, v.x, v.y, v.z, r);
+        out[0] = r[0];
+        out[1] = r[1];
+        out[2] = r[2];
+    } else {
+        out[0] = hit ? v.x : 0.f;
+    }
+}
 
 // Channel values of the rotated query at (x, y, z), rotation matrix in
 // registers; same results as sample().
