@@ -12,11 +12,12 @@ search correlates the best 5%, the exhaustive search is the fallback).  A
 step aligns a batch of held-out pairs (seeds outside the training range).
 The same pairs are also aligned with the exhaustive search: the line reports
 both rates and the fraction of pairs whose top-1 rotation the two forms
-agree on.  A step runs ``Aligner.align_many`` over its pairs: every stage is
-launched for all pairs before the host waits.  The line also reports the
-rate with the global stage (fastVEC, spectra, proposal, global search of
-every pair) replayed as one CUDA graph (``graph_replay``; ``--graph`` makes
-that the headline).
+agree on.  A step runs ``Aligner.align_many`` over its pairs with
+graph=True: the global stage (fastVEC, spectra, proposal, global search of
+every pair) and the refinement + rescoring stage each replay as one CUDA
+graph, captured in the warm-up for the batch's shapes (every kernel of the
+step still runs each step).  The line also reports the same steps with
+eager launches (``eager``; ``--eager`` makes that the headline).
 
 At one GPU the same line carries, under ``configs``, the other benchmarked
 configurations, each with its own device-timed value, end-to-end value, FP32
@@ -96,10 +97,10 @@ def parse():
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--no-exhaustive", action="store_true",
                     help="skip the exhaustive form on the same pairs (profiling runs)")
-    ap.add_argument("--graph", action="store_true",
-                    help="headline value with the global stage replayed as one CUDA graph")
+    ap.add_argument("--eager", action="store_true",
+                    help="headline value with eager launches instead of the CUDA graphs")
     ap.add_argument("--no-graph-replay", action="store_true",
-                    help="skip the CUDA-graph measurement (profiler launch lists)")
+                    help="skip the second form's measurement (eager, or graphs with --eager; profiler lists)")
     ap.add_argument("--case", nargs="+", default=None, metavar="NAME",
                     help="run one small profiling case of bench_cases.py instead of a workload")
     return ap.parse_args()
@@ -368,7 +369,8 @@ def run_gb300(args):
     dev_items = [(m1, m2, wd, wd, o1, o2) for (m1, m2, _, _, o1, o2, wd) in pairs]
     host_items = [(h1, h2, wd, wd, o1, o2) for (_, _, h1, h2, o1, o2, wd) in pairs]
 
-    graph = False
+    headline_graph = not args.eager
+    graph = headline_graph
 
     def step(params):
         flush.zero_()
@@ -393,18 +395,18 @@ def run_gb300(args):
         barrier()
         return maxr(e0.elapsed_time(e1)), res, launches, clk.stop()
 
-    # the same steps with the global stage replayed as one CUDA graph (captured
-    # in the warm-up for this batch's shapes and geometry; a batch of new maps
-    # with another grid geometry captures again)
-    ms_g = None
-    if not args.no_graph_replay or args.graph:
-        graph = True
-        ms_g, _, _, _ = timed(p)
-    graph = bool(args.graph)
+    # the same steps in the other form (eager launches, or the CUDA graphs
+    # with --eager); graphs are captured in the warm-up for this batch's shapes
+    # and geometry (a batch of new maps with other geometry captures again)
+    ms_alt = None
+    if not args.no_graph_replay:
+        graph = not headline_graph
+        ms_alt, _, _, _ = timed(p)
+    graph = headline_graph
     ms, res, launches, clocks = timed(p)
     npairs = len(pairs)
     value = world * npairs * args.steps / (ms / 1e3)
-    value_graph = world * npairs * args.steps / (ms_g / 1e3) if ms_g else None
+    value_alt = world * npairs * args.steps / (ms_alt / 1e3) if ms_alt else None
     fallbacks = 0
     if use_prop:
         # fallbacks in one step of the proposal form
@@ -425,7 +427,7 @@ def run_gb300(args):
     # ---- end to end: host maps copied in every step -------------------------
     def host_step(params):
         flush.zero_()
-        al.align_host_many(host_items, params)
+        al.align_host_many(host_items, params, graph=headline_graph)
         return al.d2h_bytes
 
     def timed_host(params):
@@ -482,15 +484,19 @@ def run_gb300(args):
         "config": {"workload": wl, "grid_sides": dims, "pairs_per_step": npairs,
                    "rotations": len(vg.calc_angle_comb(p.A)),
                    "l2": "flushed before every step (256 MB write)", "parallelism": f"replicas x{world}",
-                   "global_stage": "one CUDA graph replay per step" if args.graph else "eager launches"},
-        "graph_replay": {"value": round(value_graph, 4), "unit": UNIT, "ms_per_step": round(ms_g / args.steps, 3),
-                         "note": "global stage as one CUDA graph, captured once for this batch's shapes"}
-        if value_graph else None,
+                   "form": ("CUDA graphs: global stage, then refinement + rescoring, replayed every step "
+                            "(captured in the warm-up for this batch's shapes)") if headline_graph else
+                           "eager launches"},
+        ("eager" if headline_graph else "graphs"): {"value": round(value_alt, 4), "unit": UNIT,
+                                                    "ms_per_step": round(ms_alt / args.steps, 3)}
+        if value_alt else None,
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(d2h / args.steps)},
         "gpu_launches": int(launches),
         "roofline": roof,
         "stage_ms_profiled_step": {k: round(v, 3) for k, v in stages.items()},
+        "profiled_step_note": "one eager step with events at stage boundaries; one with events around every "
+                              "search launch (global searches)",
         "pass_ms_profiled_step": [round(x, 3) for x in prof["pass_ms"]],
         "clocks": clocks,
     }
@@ -546,7 +552,8 @@ def config_pair200(args, dev):
     steps, warmup = min(args.steps, SUB_STEPS), SUB_WARMUP
     out = {"config": {"workload": "pair200_s2_a10: one pair per step, map1 200^3 / map2 100^3 (1500 blobs, 70 A "
                                   "sphere), s=2, A=10 (24624 rotations + refinement), g=16, N=10, exhaustive; "
-                                  "headline fields from mode V",
+                                  "headline fields from mode V; CUDA graphs per step (modes CC and PCC: eager, "
+                                  "their spectra need a host value)",
                       "l2": "flushed before every step (256 MB write)"},
            "steps": steps, "warmup": warmup, "unit": UNIT, "modes": {}}
     fields_v = None
@@ -554,7 +561,7 @@ def config_pair200(args, dev):
         p = align.AlignParams(t=w["t"], T=w["T"], g=w["g"], s=w["s"], A=w["A"], N=w["N"], mode=MODE_NAMES[m])
         for _ in range(warmup):
             flush.zero_()
-            al.align_many(items, p)
+            al.align_many(items, p, graph=True)
         torch.cuda.synchronize()
         clk = ClockSampler(torch.cuda.current_device())
         clk.start()
@@ -563,7 +570,7 @@ def config_pair200(args, dev):
         for _ in range(steps):
             flush.zero_()
             e0.record()
-            res = al.align_many(items, p)
+            res = al.align_many(items, p, graph=True)
             e1.record()
             torch.cuda.synchronize()
             total += e0.elapsed_time(e1)
@@ -580,13 +587,13 @@ def config_pair200(args, dev):
                "roofline": search_roofline(prof, dev, clocks, kernel_names(dev, res[0].dim, MODE_NAMES[m])),
                "pass_ms_profiled_step": [round(x, 3) for x in prof["pass_ms"]], "clocks": clocks}
         if m == "V":
-            al.align_host_many(host_items, p)
+            al.align_host_many(host_items, p, graph=True)
             torch.cuda.synchronize()
             e0.record()
             d2h = 0
             for _ in range(steps):
                 flush.zero_()
-                al.align_host_many(host_items, p)
+                al.align_host_many(host_items, p, graph=True)
                 d2h += al.d2h_bytes
             e1.record()
             torch.cuda.synchronize()

@@ -263,6 +263,14 @@ int vesper_rescore_batch_workspace_size(int dim, int nmodel, size_t *bytes);
 int vesper_rescore_batch(const double *tdata, const float *tvec, double tave, double tstd, double tstd_norm_ave,
                          const double *sdata, const float *svec, int dim, const int32_t *trans_dev, int nmodel,
                          double *result_out, void *workspace, size_t workspace_bytes, void *stream);
+/* vesper_rescore_batch with the target's statistics read from DEVICE memory
+ * (tstats_dev: the double[5] that vesper_map_stats / vesper_map_stats_ws
+ * write; ave, L2 norm and centred L2 norm are entries 2, 3 and 4), so that a
+ * caller can record the call once and replay it for new maps without reading
+ * the statistics back to the host.  No counterpart in the reference. */
+int vesper_rescore_batch_dev(const double *tdata, const float *tvec, const double *tstats_dev, const double *sdata,
+                             const float *svec, int dim, const int32_t *trans_dev, int nmodel, double *result_out,
+                             void *workspace, size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Probability-map hole filling (interpolate, interpolation_functions.py:6-135)

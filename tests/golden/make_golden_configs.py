@@ -322,6 +322,10 @@ def combine():
             with open(os.path.join(HERE, "prob_pair128_pad64.txt"), "w") as f:
                 f.write(txt)
     if p200:
+        # jobs run separately add their modes to those already in the fixture
+        old = os.path.join(HERE, "search_pair200.npz")
+        if os.path.exists(old):
+            p200 = dict(np.load(old), **p200)
         for m in PAIR200_MODES:
             if f"{m}_stdout" in p200:
                 with open(os.path.join(HERE, f"search_pair200_{m}.txt"), "w") as f:

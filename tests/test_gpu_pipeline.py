@@ -207,7 +207,8 @@ def test_align_many_graph_replay_equals_eager(dev):
     eager = al.align_many(items, p)
     g1 = al.align_many(items, p, graph=True)
     g2 = al.align_many(items, p, graph=True)
-    assert al.graph_captures == 1 and al.graph_replays == 2
+    # two graphs per batch signature: the global stage, then refinement + rescoring
+    assert al.graph_captures == 2 and al.graph_replays == 4
     for a, b, c in zip(eager, g1, g2):
         for r in (b, c):
             assert r.top == a.top

@@ -198,8 +198,11 @@ class Aligner:
     def align_many(self, items, p: AlignParams, graph: bool = False) -> list:
         """Align a batch of pairs, items = [(src1, src2, width1, width2, orig1,
         orig2)] with device maps of any (uneven) sizes.  Every stage is launched
-        for all pairs before the host waits, so the whole batch needs about five
-        host synchronisations instead of five per pair."""
+        for all pairs before the host waits: one wait for the grid sizes, one
+        for the proposal's flatness test (learned proposal only), one for all
+        results.  With graph=True the global stage and the refinement +
+        rescoring stage each replay as one CUDA graph per batch signature
+        (modes other than CC and PCC, whose spectra need a host value)."""
         dev = self.dev
         mode = p.mode
         self.launches = 0
@@ -252,10 +255,19 @@ class Aligner:
                 st.order = None
                 st.fallback = True
                 self._global_search(p, st, mats, nang)
+                st.tg.copy_(st.top.to(st.tg.dtype))     # top grid indices, read by the device late stage
             self.proposal_info = {"subset": int(np.ceil(p.proposal_frac * nang)), "z": [float(z) for z in zs],
                                   "fallback": [bool(st.fallback) for st in P]}
         else:
             self.proposal_info = None
+        if graph and mode not in ("PCC", "CC") and p.A > 5.0 and self.group is None and \
+                self._grid_rows(p.A, angle_comb) is not None:
+            # refinement and rescoring on the device from the top indices, no
+            # host value in between, replayed as one CUDA graph.  (Eager calls
+            # keep the host-driven refinement below, which searches each
+            # distinct angle once: fewer rotations, one more host round trip.)
+            self._late_stage_graph(P, p, stats, mats)
+            return self._finish_device_late(P, p, stats, angle_comb, nang)
         if sh is None:
             sh = stats.cpu().numpy()
             self.d2h_bytes += sh.nbytes
@@ -487,10 +499,17 @@ class Aligner:
         else:
             for st in P:
                 self._global_search(p, st, mats if st.order is None else st.sub, nang)
+        for st in P:   # the global top-N as grid indices (-1: none)
+            if st.order is not None:
+                t = st.top.to(torch.int64)
+                st.tg = torch.where(t >= 0, st.order.to(torch.int64).index_select(0, t.clamp(min=0)),
+                                    torch.full_like(t, -1))
+            else:
+                st.tg = st.top.to(torch.int64)
         return stats, sh
 
     _STAGE_FIELDS = ("tdata", "tvec", "qdata", "qvec", "ave", "spec", "order", "sub", "scores", "lin", "top", "z",
-                     "launches")
+                     "tg", "launches")
 
     def _global_stage_graph(self, P, p, mats, nang):
         """_global_stage through a CUDA graph cached by the batch's signature
@@ -498,11 +517,7 @@ class Aligner:
         batch replays one graph instead of its hundreds of launches.  A new
         signature runs the stage once eagerly (autotuning, first launches),
         then captures it."""
-        sig = (tuple((st.src1.data_ptr(), st.src2.data_ptr(), tuple(st.src1.shape), tuple(st.src2.shape), st.dim,
-                      tuple(np.asarray(st.no1, np.float64)), tuple(np.asarray(st.no2, np.float64)),
-                      float(st.width1), float(st.width2), tuple(st.o1), tuple(st.o2)) for st in P),
-               (p.t, p.T, p.g, p.s, p.A, p.N, p.mode, p.batch, id(p.proposal), p.proposal_frac, p.proposal_pool),
-               mats.data_ptr())
+        sig = self._batch_sig(P, p, mats)
         ent = self._graphs.get(sig)
         if ent is None:
             base = [st.launches for st in P]
@@ -533,6 +548,196 @@ class Aligner:
                     setattr(st, k, sv[k])
         self.graph_replays += 1
         return stats
+
+    @staticmethod
+    def _batch_sig(P, p, mats):
+        """What a captured stage depends on: input addresses and shapes, grid
+        geometry, parameters, the angle grid."""
+        return (tuple((st.src1.data_ptr(), st.src2.data_ptr(), tuple(st.src1.shape), tuple(st.src2.shape), st.dim,
+                       tuple(np.asarray(st.no1, np.float64)), tuple(np.asarray(st.no2, np.float64)),
+                       float(st.width1), float(st.width2), tuple(st.o1), tuple(st.o2)) for st in P),
+                (p.t, p.T, p.g, p.s, p.A, p.N, p.mode, p.batch, id(p.proposal), p.proposal_frac, p.proposal_pool),
+                mats.data_ptr())
+
+    # ---- refinement and rescoring on the device ---------------------------------
+    # The +-5 degree refinement set of a top angle is its 27 neighbours on the
+    # 5-degree lattice in the reference's meshgrid order, kept where x < 360,
+    # y < 360 and z < 180 and wrapped by +360 where negative (:689-713).  Every
+    # pair gets N x 27 slots in that order, the slots the filter drops marked
+    # invalid and left out of the top-N (their score reads -inf), so the stable
+    # top-N over the slots is the reference's over its list, duplicates
+    # included.  The models' rotations are rows of the lattice table, their
+    # translations come from the search's linear index, and the float64
+    # rescoring reads the target statistics from the device: nothing in the
+    # stage needs a host value, so it replays as one CUDA graph.
+
+    def _grid_rows(self, A, angle_comb):
+        """Device int64 lattice rows of the angle grid's angles, or None when
+        the grid is off the 5-degree lattice."""
+        cache = self.__dict__.setdefault("_grid_rows_cache", {})
+        if A not in cache:
+            idx = vg.lattice_index(angle_comb)
+            cache[A] = None if idx is None else self.dev.to_dev(np.asarray(idx, np.int64))
+        return cache[A]
+
+    def _ref_offsets(self):
+        t = self.__dict__.get("_ref_off")
+        if t is None:
+            t = self._ref_off = self.dev.to_dev((vg._REFINE_OFFSETS // 5).astype(np.int64))   # [27, 3] lattice steps
+        return t
+
+    def _late_stage(self, P, p, stats):
+        dev = self.dev
+        mode = p.mode
+        L = vg.LATTICE_N
+        n, N = len(P), p.N
+        lat = vg.lattice_rot_matrices_device(dev)
+        grid_rows = self._grid_rows(p.A, None)
+        off = self._ref_offsets()
+        self._mark("refine")
+        tg = torch.stack([st.tg for st in P])                                  # [n, N] grid indices
+        rows = grid_rows.index_select(0, tg.clamp(min=0).reshape(-1)).reshape(n, N)
+        base = torch.stack([rows // (L * L), (rows // L) % L, rows % L], dim=2)  # [n, N, 3]
+        cand = base[:, :, None, :] + off[None, None, :, :]                     # [n, N, 27, 3]
+        valid = (cand[..., 0] < L) & (cand[..., 1] < L) & (cand[..., 2] < L // 2) & (tg >= 0)[:, :, None]
+        cand = torch.where(cand < 0, cand + L, cand)
+        crow = (cand[..., 0] * L + cand[..., 1]) * L + cand[..., 2]
+        valid = valid.reshape(n, N * 27)
+        crow = torch.where(valid, crow.reshape(n, N * 27), torch.zeros_like(valid, dtype=torch.int64))
+        rmats = lat.index_select(0, crow.reshape(-1)).reshape(n, N * 27, 3, 3)
+        nscore = dev.lib.vesper_search_nscore(vg.MODE_CODES[mode], 0)
+        RS = torch.empty((n, N * 27, nscore), dtype=torch.float32, device=dev.device)
+        RL = torch.empty((n, N * 27, nscore), dtype=torch.int32, device=dev.device)
+        for i, st in enumerate(P):
+            vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats[i], batch=p.batch, dev=dev, tuned=True,
+                             out=(RS[i], RL[i]))
+            st.launches += self._search_launches(st.dim, mode, N * 27, p.batch)
+        masked = torch.where(valid, RS[:, :, 0], torch.full_like(RS[:, :, 0], float("-inf")))
+        rtop = torch.stack([vg.topn_device(masked[i].contiguous(), N, dev=dev) for i in range(n)])   # [n, N]
+        sel = rtop.to(torch.int64).clamp(min=0)
+        r_rows = crow.gather(1, sel)
+        r_score = RS[:, :, 0].gather(1, sel)
+        r_lin = RL[:, :, 0].to(torch.int64).gather(1, sel)
+        mm = lat.index_select(0, r_rows.reshape(-1)).reshape(n, N, 3, 3)
+        self._mark("rescore")
+        for i, st in enumerate(P):
+            d = st.dim
+            st.launches += 1
+            st.rtop, st.r_rows, st.r_score, st.r_lin = rtop[i], r_rows[i], r_score[i], r_lin[i]
+            gd, gv, _ = vg.rot_gather_device(st.qdata, st.qvec, mm[i], dev=dev)
+            lin = r_lin[i]
+            t = torch.stack([lin // (d * d), (lin // d) % d, lin % d], dim=1)
+            trd = torch.where(2 * t > d, t - d, t).to(torch.int32).contiguous()   # wrapped as get_score (:1323-1329)
+            st.res = torch.empty((N, 8), dtype=torch.float64, device=dev.device)
+            ws = dev.workspace(("rescore_batch", i, d, N), _native.size_query("vesper_rescore_batch_workspace_size", d, N))
+            _native.check(self.lib.vesper_rescore_batch_dev(
+                ctypes.c_void_p(st.tdata.data_ptr()), ctypes.c_void_p(st.tvec.data_ptr()),
+                ctypes.c_void_p(stats[i].data_ptr()), ctypes.c_void_p(gd.data_ptr()), ctypes.c_void_p(gv.data_ptr()),
+                d, ctypes.c_void_p(trd.data_ptr()), N, ctypes.c_void_p(st.res.data_ptr()),
+                ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
+            st.launches += 5
+            if self.pair_events is not None and not torch.cuda.is_current_stream_capturing():
+                e = torch.cuda.Event(enable_timing=True)
+                e.record()
+                self.pair_events.append(e)
+
+    _LATE_FIELDS = ("rtop", "r_rows", "r_score", "r_lin", "res", "launches")
+
+    def _late_stage_graph(self, P, p, stats, mats):
+        """_late_stage through a CUDA graph cached by the batch's signature
+        (its inputs are the global stage graph's outputs, at fixed addresses)."""
+        sig = self._batch_sig(P, p, mats)
+        graphs = self.__dict__.setdefault("_late_graphs", {})
+        ent = graphs.get(sig)
+        if ent is None:
+            base = [st.launches for st in P]
+            marks, events = self.stages, self.pair_events
+            self._late_stage(P, p, stats)                   # warm-up: tunes, loads kernels, sizes workspaces
+            self.stages, self.pair_events = None, None
+            for st, b0 in zip(P, base):
+                st.launches = b0
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._late_stage(P, p, stats)
+            self.stages, self.pair_events = marks, events
+            saved = []
+            for st, b0 in zip(P, base):
+                sv = {k: getattr(st, k) for k in self._LATE_FIELDS}
+                sv["launches"] = st.launches - b0
+                st.launches = b0
+                saved.append(sv)
+            ent = graphs[sig] = (g, saved)
+            self.graph_captures += 1
+        g, saved = ent
+        self._mark("refine")
+        g.replay()
+        for st, sv in zip(P, saved):
+            for k in self._LATE_FIELDS:
+                if k == "launches":
+                    st.launches += sv[k]
+                else:
+                    setattr(st, k, sv[k])
+        if self.pair_events is not None:   # every pair ends with the graph
+            e = torch.cuda.Event(enable_timing=True)
+            e.record()
+            self.pair_events.extend([e] * len(P))
+        self.graph_replays += 1
+
+    def _finish_device_late(self, P, p, stats, angle_comb, nang):
+        """One wait for every pair's global and refined results, then the host
+        bookkeeping: statistics and top-N list of the global pass, refined
+        models and their scores."""
+        mode = p.mode
+        L = vg.LATTICE_N
+        self._mark("results")
+        groups = [[st.scores[:, 0].contiguous(), st.lin[:, 0].contiguous(), st.top,
+                   st.rtop, st.r_rows, st.r_score, st.r_lin, st.res] +
+                  ([st.order] if st.order is not None else []) for st in P]
+        groups.append([stats])
+        h = self._fetch(groups)
+        sh = h[-1][0]
+        out = []
+        for i, st in enumerate(P):
+            raw, lin_h, top, rtop, r_rows, r_score, r_lin, res = h[i][:8]
+            order = h[i][8] if st.order is not None else None
+            rd3 = 1.0 / st.dim ** 3
+            scale = 1.0
+            if mode == "CC":
+                scale = 1.0 / sh[i, 3] ** 2
+            elif mode == "PCC":
+                scale = 1.0 / sh[i, 4] ** 2
+            top_h = [int(t) for t in top if t >= 0]
+            raw_grid, lin_grid = raw, lin_h
+            if order is not None:
+                top_h = [int(order[t]) for t in top_h]   # subset positions -> grid indices
+                raw_grid = np.zeros(nang, raw.dtype)
+                lin_grid = np.zeros(nang, lin_h.dtype)
+                raw_grid[order] = raw
+                lin_grid[order] = lin_h
+            score_arr = raw.astype(np.float64) * scale * rd3
+            ave_s, std_s = float(np.mean(score_arr)), float(np.std(score_arr))
+            score_grid = raw_grid.astype(np.float64) * scale * rd3
+            top_list = [(tuple(angle_comb[r]), float(score_grid[r]), vg.unravel(lin_grid[r], st.dim)) for r in top_h]
+            models = []
+            for k in range(len(rtop)):
+                if rtop[k] < 0:
+                    continue
+                row = int(r_rows[k])
+                ang = (float(row // (L * L)) * vg.LATTICE_STEP, float((row // L) % L) * vg.LATTICE_STEP,
+                       float(row % L) * vg.LATTICE_STEP)
+                ang = tuple(np.float64(a) for a in ang)
+                sc = float(np.float64(r_score[k]) * scale * rd3)
+                tr = vg.unravel(int(r_lin[k]), st.dim)
+                nm, total = res[k, 0], res[k, 1]
+                models.append(Model(ang, sc, tr, float(nm / total), float(res[k, 2]), float(res[k, 3]),
+                                    float(res[k, 4]), (st.c1, st.c2, p.s, st.dim)))
+            self.launches += st.launches
+            out.append(AlignResult(st.dim, std_s, ave_s, top_list, models, st.launches))
+        self.last_fields = [{"tdata": st.tdata, "tvec": st.tvec, "qdata": st.qdata, "qvec": st.qvec,
+                             "ave": float(st.ave)} for st in P]
+        self._mark("end")
+        self._close_marks()
+        return out
 
     def _fetch(self, groups):
         """Device tensors (a list of lists) to numpy with one copy and one

@@ -159,7 +159,16 @@ struct RescoreBatchArgs {
     double *stats;         // [nmodel][4]: n2, ave2, std2, nt
     double *result;        // [nmodel][8]
     double *sco;           // [vol] (nmodel == 1 only) or NULL
+    const double *tstats;  // DEVICE vesper_map_stats layout of the target, or NULL: tave/tstd/tstd_norm_ave
 };
+
+// Target statistics: from device memory when given (so that a captured call
+// replays with new maps), else the host values.
+__device__ __forceinline__ double rb_tave(const RescoreBatchArgs &a) { return a.tstats ? a.tstats[2] : a.tave; }
+__device__ __forceinline__ double rb_tstd(const RescoreBatchArgs &a) { return a.tstats ? a.tstats[3] : a.tstd; }
+__device__ __forceinline__ double rb_tpstd(const RescoreBatchArgs &a) {
+    return a.tstats ? a.tstats[4] : a.tstd_norm_ave;
+}
 
 __device__ __forceinline__ void rb_chunk(const RescoreBatchArgs &a, size_t &lo, size_t &hi) {
     const size_t vol = (size_t)a.d * a.d * a.d;
@@ -223,6 +232,7 @@ __global__ void __launch_bounds__(kRbThreads) k_rescore_p2(const RescoreBatchArg
     const double *sd = a.sdata + (size_t)m * vol;
     const float *sv = a.svec + (size_t)m * vol * 3;
     const double ave2 = a.stats[(size_t)m * 4 + 1];
+    const double tave = rb_tave(a);
     const int tx = a.trans ? a.trans[3 * m] : a.tx, ty = a.trans ? a.trans[3 * m + 1] : a.ty,
               tz = a.trans ? a.trans[3 * m + 2] : a.tz;
     size_t lo, hi;
@@ -241,7 +251,7 @@ __global__ void __launch_bounds__(kRbThreads) k_rescore_p2(const RescoreBatchArg
         const double t = a.tdata[i], s = sd[j];
         const double d1 = t <= 0 ? 0.0 : t;
         const double d2 = s <= 0 ? 0.0 : d1;   // the reference's d2 = where(d2 <= 0, 0, d1)
-        const double pd1 = d1 <= 0 ? 0.0 : d1 - a.tave;
+        const double pd1 = d1 <= 0 ? 0.0 : d1 - tave;
         const double pd2 = d2 <= 0 ? 0.0 : d2 - ave2;
         cc += d1 * d2;
         pcc += pd1 * pd2;
@@ -282,8 +292,8 @@ __global__ void k_rescore_r2(const RescoreBatchArgs a) {
     double *r = a.result + (size_t)m * 8;
     r[0] = acc[3];
     r[1] = st[3] + acc[4];
-    r[2] = acc[1] / (a.tstd * st[2]);
-    r[3] = acc[2] / (a.tstd_norm_ave * pstd2);
+    r[2] = acc[1] / (rb_tstd(a) * st[2]);
+    r[3] = acc[2] / (rb_tpstd(a) * pstd2);
     r[4] = acc[5];
     r[5] = st[1];
     r[6] = st[2];
@@ -359,7 +369,30 @@ extern "C" int vesper_rescore_batch(const double *tdata, const float *tvec, doub
     double *part = cv.take<double>((size_t)nmodel * nchunk * kRbParts);
     double *stats = cv.take<double>((size_t)nmodel * 4);
     RescoreBatchArgs a{tdata, tvec, tave, tstd, tstd_norm_ave, sdata, svec, dim, nmodel, nchunk, trans_dev,
-                       0, 0, 0, part, stats, result_out, nullptr};
+                       0, 0, 0, part, stats, result_out, nullptr, nullptr};
+    return launch_rescore_batch(a, (cudaStream_t)stream);
+}
+
+extern "C" int vesper_rescore_batch_dev(const double *tdata, const float *tvec, const double *tstats_dev,
+                                        const double *sdata, const float *svec, int dim, const int32_t *trans_dev,
+                                        int nmodel, double *result_out, void *workspace, size_t workspace_bytes,
+                                        void *stream) {
+    if (!tstats_dev) return fail(VESPER_ERR_INVALID, "vesper_rescore_batch_dev: missing target statistics");
+    if (!tdata || !tvec || !sdata || !svec || !trans_dev || !result_out)
+        return fail(VESPER_ERR_INVALID, "vesper_rescore_batch_dev: missing pointer");
+    if (dim < 1 || nmodel < 0 || nmodel > 65535)
+        return fail(VESPER_ERR_INVALID, "vesper_rescore_batch_dev: bad sizes");
+    if (nmodel == 0) return VESPER_OK;
+    size_t need = 0;
+    vesper_rescore_batch_workspace_size(dim, nmodel, &need);
+    if (!workspace || workspace_bytes < need)
+        return fail(VESPER_ERR_WORKSPACE, "vesper_rescore_batch_dev: workspace");
+    const int nchunk = (int)rescore_chunks(dim);
+    Carver cv(workspace, workspace_bytes);
+    double *part = cv.take<double>((size_t)nmodel * nchunk * kRbParts);
+    double *stats = cv.take<double>((size_t)nmodel * 4);
+    RescoreBatchArgs a{tdata, tvec, 0.0, 0.0, 0.0, sdata, svec, dim, nmodel, nchunk, trans_dev,
+                       0, 0, 0, part, stats, result_out, nullptr, tstats_dev};
     return launch_rescore_batch(a, (cudaStream_t)stream);
 }
 
