@@ -263,7 +263,8 @@ __global__ void __launch_bounds__(256, rpass_a_ctas<MODE, N1, N2>()) k_rpass_a(c
 // Pass A for sides up to 32 with whole lines in registers: PL x-planes per
 // CTA; one packed z line per thread (DFT + unpack in registers), then one y
 // column per thread (DFT in registers, straight to S).
-constexpr int kLinePlanes = 2;   // x-planes per CTA of the whole-line passes
+constexpr int kLinePlanes = 1;     // x-planes per CTA of the whole-line pass A
+constexpr int kLineAThreads = 64;   // its block size (measured: 64 threads, 1 plane beat 128 and 256 threads, 2 planes)
 
 template <int D>
 struct LineGeom {
@@ -277,7 +278,7 @@ __host__ __device__ inline size_t smem_ra_line() {
 }
 
 template <int MODE, int NCH, int N1, int N2, int PL>
-__global__ void __launch_bounds__(256, 2) k_rpass_a_line(const PassA2 a) {
+__global__ void __launch_bounds__(kLineAThreads, 8) k_rpass_a_line(const PassA2 a) {
     constexpr int D = N1 * N2;
     using L = LineGeom<D>;
     constexpr int H = L::H, NP = L::NP, Hp = L::Hp, LS = L::LS, PS = L::PS;
@@ -426,7 +427,7 @@ __global__ void __launch_bounds__(256) k_rpass_b(const PassB2 a) {
 // ky H + kz per thread, whole x lines in registers -- for every channel the
 // forward x DFT of its S column, times conj(T) added into the column's sum,
 // then the inverse x DFT of the sum straight to U.  No shared memory.
-constexpr int kLineBThreads = 128;
+constexpr int kLineBThreads = 64;  // fewer idle threads in the last CTA of each rotation (measured: 64 beat 128, 256)
 
 template <int NCH, int N1, int N2>
 __global__ void __launch_bounds__(kLineBThreads) k_rpass_b_line(const PassB2 a) {
@@ -593,7 +594,7 @@ struct RegPath {
             constexpr int PL = kLinePlanes;
             const size_t sl = smem_ra_line<N1 * N2, NCH, PL>();
             allow_smem(k_rpass_a_line<MODE, NCH, N1, N2, PL>, sl);
-            k_rpass_a_line<MODE, NCH, N1, N2, PL><<<dim3((N1 * N2 + PL - 1) / PL, g.y), 256, sl, st>>>(p);
+            k_rpass_a_line<MODE, NCH, N1, N2, PL><<<dim3((N1 * N2 + PL - 1) / PL, g.y), kLineAThreads, sl, st>>>(p);
         } else {
             allow_smem(k_rpass_a<MODE, NCH, N1, N2>, s);
             k_rpass_a<MODE, NCH, N1, N2><<<g, T, s, st>>>(p);
