@@ -101,6 +101,9 @@ def parse():
                     help="headline value with eager launches instead of the CUDA graphs")
     ap.add_argument("--no-graph-replay", action="store_true",
                     help="skip the second form's measurement (eager, or graphs with --eager; profiler lists)")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="run one more step of the headline form between cudaProfilerStart and cudaProfilerStop "
+                         "(for ncu --profile-from-start off: a launch list of exactly one step)")
     ap.add_argument("--case", nargs="+", default=None, metavar="NAME",
                     help="run one small profiling case of bench_cases.py instead of a workload")
     return ap.parse_args()
@@ -404,6 +407,12 @@ def run_gb300(args):
         ms_alt, _, _, _ = timed(p)
     graph = headline_graph
     ms, res, launches, clocks = timed(p)
+    if args.profile_step:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        step(p)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     npairs = len(pairs)
     value = world * npairs * args.steps / (ms / 1e3)
     value_alt = world * npairs * args.steps / (ms_alt / 1e3) if ms_alt else None
@@ -417,6 +426,11 @@ def run_gb300(args):
     al.stages = stages       # stage boundaries only: events between stages (eager launches)
     al.align_many(dev_items, p)
     barrier()
+    stages_graph = {}
+    if not args.no_graph_replay or headline_graph:
+        al.stages = stages_graph     # the same in the graph form: the two replays and the host work around them
+        al.align_many(dev_items, p, graph=True)
+        barrier()
     al.stages = None
     prof = {}
     al.profile = prof        # events around every search launch (slower; its own step)
@@ -495,8 +509,10 @@ def run_gb300(args):
         "gpu_launches": int(launches),
         "roofline": roof,
         "stage_ms_profiled_step": {k: round(v, 3) for k, v in stages.items()},
-        "profiled_step_note": "one eager step with events at stage boundaries; one with events around every "
-                              "search launch (global searches)",
+        "stage_ms_graph_step": {k: round(v, 3) for k, v in stages_graph.items()},
+        "profiled_step_note": "one eager step with events at stage boundaries; one graph-form step with events "
+                              "between its two replays; one with events around every search launch (global "
+                              "searches)",
         "pass_ms_profiled_step": [round(x, 3) for x in prof["pass_ms"]],
         "clocks": clocks,
     }

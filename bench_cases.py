@@ -5,8 +5,8 @@ through ``python bench.py --case <name> [arg]``:
       three register/fused-path searches of seeded random side-d fields over
       the first nrot (default 1008) rotations of the 30-degree grid
   prop
-      three learned-proposal scorings (committed weights) of one held-out
-      128^3 / 64^3 pair at s = 3 over the 10-degree grid
+      learned-proposal scorings (committed weights) of one held-out
+      128^3 / 64^3 pair at s = 3 over the 10-degree grid, timed
   cufft<d> [nrot]
       comparison only: the FFT work of a mode-V search through cuFFT
       (torch.fft, no gather) next to this library's whole search, per rotation
@@ -189,8 +189,15 @@ def main(argv=None):
         maker = P.PairMaker(dev)
         mats = vg.rot_matrices_device(vg.calc_angle_comb(10.0), dev, key=("grid", 10.0))
         pf = maker.fields(30_000_000)
+        net.rotation_scores(pf.fTQ, mats)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
         for _ in range(3):
             net.rotation_scores(pf.fTQ, mats)
+        e1.record()
+        torch.cuda.synchronize()
+        print(f"proposal scores of one pair, {int(mats.shape[0])} rotations: {e0.elapsed_time(e1) / 3:.3f} ms "
+              f"(encoder and scoring)")
     else:
         raise SystemExit(f"unknown case {what!r}")
     torch.cuda.synchronize()

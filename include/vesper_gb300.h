@@ -76,6 +76,12 @@ int vesper_fast_len_ok(int n);
  * ------------------------------------------------------------------------- */
 int vesper_prepare_map(float *data, int sx, int sy, int sz, double threshold, const double *cent, uint64_t *out2,
                        void *stream);
+/* vesper_prepare_map for nmap maps in one launch (per 64 maps): HOST arrays
+ * data[nmap] (device pointers), dims[3 nmap], thresholds[nmap], cents[3 nmap];
+ * out is DEVICE uint64[2 nmap], map i's pair at out[2i] -- the same values as
+ * nmap calls of vesper_prepare_map. */
+int vesper_prepare_maps(int nmap, float *const *data, const int *dims, const double *thresholds, const double *cents,
+                        uint64_t *out, void *stream);
 
 /* fastVEC statistics of a d^3 float64 density (VESPER_1_prob_new.py:157-161):
  * stats_out DEVICE double[5] = {sum, count != 0, mean of > 0, L2 norm of > 0,
@@ -332,6 +338,12 @@ int vesper_prop_score_f16(const void *ET, const void *EQ, int K, int d, const fl
 int vesper_prop_srcmap(int d, const float *rotmats, int nrot, void *srcmap_out, void *stream);
 int vesper_prop_score_map(const void *ET, const void *EQ, int K, int d, const void *srcmap, int nrot,
                           float *scores, void *stream);
+/* vesper_prop_score_map for npair pairs of one grid side in one launch: VM is
+ * float16 voxel-major [2 npair][d^3][K] (pair i: target map 2i, query map
+ * 2i + 1), scores float32 [npair][nrot]; the same scores as npair calls of
+ * vesper_prop_score_map, bit for bit. */
+int vesper_prop_score_map_many(const void *VM, int npair, int K, int d, const void *srcmap, int nrot,
+                               float *scores, void *stream);
 int vesper_prop_score_bwd_workspace(int K, int d, size_t *bytes);
 /* Gradients of sum_r gscores[r] * scores[r]; gET, gEQ ACCUMULATE (+=). */
 int vesper_prop_score_bwd(const float *ET, const float *EQ, int K, int d, const float *rotmats, int nrot,

@@ -261,3 +261,47 @@ def test_interpolation_cli(dev, tmp_path, golden_dir):
         np.testing.assert_array_equal(m.data[:nz - 2, :ny - 2, :nx - 2],
                                       np.transpose(g["out0"][:nx - 2, :ny - 2, :nz - 2, c], (2, 1, 0)))
         assert tuple(m.origin) == (1.0, 2.0, 3.0)
+
+
+def test_prepare_maps_equals_per_map(dev):
+    """vesper_prepare_maps (one launch per 64 maps) thresholds every map in
+    place and gives each map's (radius bits, count) as vesper_prepare_map
+    does: uneven shapes, an all-zero map, a negative threshold, and more
+    maps than one launch takes."""
+    import ctypes
+    from vesper_python_gb300 import _native
+    from vesper_python_gb300 import vesper as vg
+    rng = np.random.default_rng(7)
+    shapes = [(17, 20, 23), (64, 64, 64), (5, 1, 9), (8, 8, 8), (33, 2, 40)] + [(6, 7, 5)] * 66
+    maps, ths = [], []
+    for i, sh in enumerate(shapes):
+        a = rng.uniform(-0.5, 1.0, size=sh).astype(np.float32)
+        a[rng.random(sh) < 0.4] = 0
+        if i == 3:
+            a[:] = 0
+        maps.append(a)
+        ths.append(-1.0 if i == 2 else float(rng.uniform(0.0, 0.6)))
+    cents = [np.array([x * 0.5 for x in sh]) + (0.25 if i % 2 else 0.0) for i, sh in enumerate(shapes)]
+    # per map
+    ref_data, ref_out = [], []
+    for a, th, c in zip(maps, ths, cents):
+        t = dev.to_dev(a)
+        o = torch.empty(2, dtype=torch.int64, device=dev.device)
+        _native.check(dev.lib.vesper_prepare_map(ctypes.c_void_p(t.data_ptr()), *a.shape, th, vg._host_d3(c),
+                                                 ctypes.c_void_p(o.data_ptr()), dev.stream))
+        ref_data.append(t.cpu().numpy())
+        ref_out.append(o.cpu().numpy())
+    # all at once
+    ts = [dev.to_dev(a) for a in maps]
+    nm = len(ts)
+    out = torch.full((nm, 2), -1, dtype=torch.int64, device=dev.device)
+    ptrs = (ctypes.c_void_p * nm)(*[t.data_ptr() for t in ts])
+    dims = (ctypes.c_int * (3 * nm))(*[v for a in maps for v in a.shape])
+    thr = (ctypes.c_double * nm)(*ths)
+    cen = (ctypes.c_double * (3 * nm))(*[float(v) for c in cents for v in c])
+    _native.check(dev.lib.vesper_prepare_maps(nm, ptrs, dims, thr, cen, ctypes.c_void_p(out.data_ptr()), dev.stream))
+    got = out.cpu().numpy()
+    for i in range(nm):
+        np.testing.assert_array_equal(got[i], ref_out[i], err_msg=f"map {i}")
+        np.testing.assert_array_equal(ts[i].cpu().numpy(), ref_data[i], err_msg=f"map {i}")
+    assert got[3, 1] == 0 and got[3, 0] == 0

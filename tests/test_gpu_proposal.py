@@ -316,3 +316,32 @@ def test_srcmap_scores_match_direct_scores(dev, d):
     smt = P.srcmap(dev, d, mats)
     _native.check(dev.lib.vesper_prop_score_map(p(vm[0]), p(vm[1]), K, d, p(smt), len(angles), p(b), dev.stream))
     np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+
+
+@pytest.mark.parametrize("d,K,npair", [(7, 8, 3), (16, 8, 4), (11, 16, 2), (16, 32, 2)])
+def test_score_map_many_matches_per_pair(dev, d, K, npair):
+    """vesper_prop_score_map_many scores every pair of one side in one launch
+    (query features staged in shared memory; at d = 16, K = 32 they do not
+    fit and each pair takes the unstaged kernel) with the direct kernel's
+    scores bit for bit, over a rotation count that leaves a partial chunk."""
+    import ctypes
+    from vesper_python_gb300 import _native
+    P = _prop()
+    from vesper_python_gb300 import vesper as vg
+    rng = np.random.default_rng(100 + d)
+    angles = orc.calc_angle_comb(30.0)[::5][:203]
+    mats = dev.to_dev(vg.rot_matrices(angles))
+    n = len(angles)
+    vm = dev.to_dev(rng.normal(size=(2 * npair, d ** 3, K)), torch.float16)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    ref = torch.empty((npair, n), device=dev.device)
+    for i in range(npair):
+        _native.check(dev.lib.vesper_prop_score_f16(p(vm[2 * i]), p(vm[2 * i + 1]), K, d, p(mats), n, p(ref[i]),
+                                                    dev.stream))
+    smt = P.srcmap(dev, d, mats)
+    got = torch.full((npair, n), float("nan"), device=dev.device)
+    _native.check(dev.lib.vesper_prop_score_map_many(p(vm), npair, K, d, p(smt), n, p(got), dev.stream))
+    np.testing.assert_array_equal(got.cpu().numpy(), ref.cpu().numpy())
+    one = torch.full((n,), float("nan"), device=dev.device)
+    _native.check(dev.lib.vesper_prop_score_map(p(vm[2]), p(vm[3]), K, d, p(smt), n, p(one), dev.stream))
+    np.testing.assert_array_equal(one.cpu().numpy(), ref[1].cpu().numpy())

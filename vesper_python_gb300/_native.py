@@ -104,6 +104,7 @@ SIGNATURES = {
     "vesper_fast_len_ok": [_i],
     "vesper_fp32_peak_probe": [_i, _i, _i, _vp, _vp, _vp],
     "vesper_prepare_map": [_vp, _i, _i, _i, _d, _vp, _vp, _vp],
+    "vesper_prepare_maps": [_i, _vp, _vp, _vp, _vp, _vp, _vp],
     "vesper_map_stats": [_vp, _i, _vp, _vp],
     "vesper_map_stats_workspace_size": [_i, _psz],
     "vesper_map_stats_ws": [_vp, _i, _vp, _vp, _sz, _vp],
@@ -137,6 +138,7 @@ SIGNATURES = {
     "vesper_prop_score_f16": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
     "vesper_prop_srcmap": [_i, _vp, _i, _vp, _vp],
     "vesper_prop_score_map": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
+    "vesper_prop_score_map_many": [_vp, _i, _i, _i, _vp, _i, _vp, _vp],
     "vesper_prop_conv_bwd": [_vp, _vp, _i, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp],
     "vesper_prop_score": [_vp, _vp, _i, _i, _vp, _i, _vp, _vp],
     "vesper_prop_score_bwd_workspace": [_i, _i, _psz],

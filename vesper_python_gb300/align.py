@@ -191,6 +191,20 @@ class Aligner:
                                                   vg._host_d3(cent), ctypes.c_void_p(out.data_ptr()),
                                                   self.dev.stream))
 
+    def _prepare_all(self, P, p, prep):
+        """vesper_prepare_maps over both maps of every pair: map 2i is pair
+        i's first map, 2i + 1 its second; prep [n][4] receives their
+        (radius bits, count) pairs in that order."""
+        maps = [(st.src1, p.t, st.cent1) for st in P]
+        maps = [m for st, m1 in zip(P, maps) for m in (m1, (st.src2, p.T, st.cent2))]
+        nm = len(maps)
+        ptrs = (ctypes.c_void_p * nm)(*[m[0].data_ptr() for m in maps])
+        dims = (ctypes.c_int * (3 * nm))(*[int(v) for m in maps for v in m[0].shape])
+        ths = (ctypes.c_double * nm)(*[float(m[1]) for m in maps])
+        cents = (ctypes.c_double * (3 * nm))(*[float(v) for m in maps for v in m[2]])
+        _native.check(self.lib.vesper_prepare_maps(nm, ptrs, dims, ths, cents, ctypes.c_void_p(prep.data_ptr()),
+                                                   self.dev.stream))
+
     def align_device(self, src1, src2, width1, width2, orig1, orig2, p: AlignParams) -> AlignResult:
         """One pair: ``align_many`` with a batch of one."""
         return self.align_many([(src1, src2, width1, width2, orig1, orig2)], p)[0]
@@ -214,12 +228,11 @@ class Aligner:
         # ---- 1. threshold + radius (device), grid sizing (host) ----------------
         self._mark("prepare")
         prep = torch.empty((n, 4), dtype=torch.int64, device=dev.device)
-        for i, st in enumerate(P):
+        for st in P:
             st.cent1 = np.array([x * 0.5 for x in st.src1.shape])
             st.cent2 = np.array([x * 0.5 for x in st.src2.shape])
-            self._prepare(st.src1, p.t, st.cent1, prep[i, 0:2])
-            self._prepare(st.src2, p.T, st.cent2, prep[i, 2:4])
-            st.launches += 4
+        self._prepare_all(P, p, prep)
+        P[0].launches += (2 * n + 63) // 64      # one launch per 64 maps
         prh = prep.cpu().numpy().view(np.uint64)
         self.d2h_bytes += prep.numel() * 8
         # ---- 2. fastVEC, target statistics and spectra -------------------------
@@ -234,7 +247,11 @@ class Aligner:
             else:
                 st.dim = d2
                 st.no1 = st.c1 - 0.5 * p.s * st.dim
-        angle_comb = vg.calc_angle_comb(p.A)
+        grids = self.__dict__.setdefault("_angle_grid_cache", {})   # the angle grid per step, read-only
+        angle_comb = grids.get(float(p.A))
+        if angle_comb is None:
+            angle_comb = grids[float(p.A)] = vg.calc_angle_comb(p.A)
+            angle_comb.setflags(write=False)
         nang = len(angle_comb)
         mats = vg.rot_matrices_device(angle_comb, dev, key=("grid", float(p.A)))
         if p.proposal is not None and mode != "VecProduct":
@@ -697,6 +714,7 @@ class Aligner:
         h = self._fetch(groups)
         sh = h[-1][0]
         out = []
+        angles = self._angle_tuples(p.A, angle_comb)
         for i, st in enumerate(P):
             raw, lin_h, top, rtop, r_rows, r_score, r_lin, res = h[i][:8]
             order = h[i][8] if st.order is not None else None
@@ -706,31 +724,27 @@ class Aligner:
                 scale = 1.0 / sh[i, 3] ** 2
             elif mode == "PCC":
                 scale = 1.0 / sh[i, 4] ** 2
-            top_h = [int(t) for t in top if t >= 0]
-            raw_grid, lin_grid = raw, lin_h
-            if order is not None:
-                top_h = [int(order[t]) for t in top_h]   # subset positions -> grid indices
-                raw_grid = np.zeros(nang, raw.dtype)
-                lin_grid = np.zeros(nang, lin_h.dtype)
-                raw_grid[order] = raw
-                lin_grid[order] = lin_h
+            tpos = [t for t in top.tolist() if t >= 0]      # positions in the searched rotations
+            top_h = [int(order[t]) for t in tpos] if order is not None else tpos   # -> grid indices
             score_arr = raw.astype(np.float64) * scale * rd3
             ave_s, std_s = float(np.mean(score_arr)), float(np.std(score_arr))
-            score_grid = raw_grid.astype(np.float64) * scale * rd3
-            top_list = [(tuple(angle_comb[r]), float(score_grid[r]), vg.unravel(lin_grid[r], st.dim)) for r in top_h]
+            # the score of grid index order[t] is that of position t (float32 -> float64, * scale * rd3)
+            top_list = [(angles[r], float(np.float64(raw[t]) * scale * rd3), vg.unravel(lin_h[t], st.dim))
+                        for t, r in zip(tpos, top_h)]
             models = []
-            for k in range(len(rtop)):
-                if rtop[k] < 0:
+            rows_l, score_l, lin_l, res_l = r_rows.tolist(), r_score.tolist(), r_lin.tolist(), res.tolist()
+            for k, rk in enumerate(rtop.tolist()):
+                if rk < 0:
                     continue
-                row = int(r_rows[k])
-                ang = (float(row // (L * L)) * vg.LATTICE_STEP, float((row // L) % L) * vg.LATTICE_STEP,
-                       float(row % L) * vg.LATTICE_STEP)
-                ang = tuple(np.float64(a) for a in ang)
-                sc = float(np.float64(r_score[k]) * scale * rd3)
-                tr = vg.unravel(int(r_lin[k]), st.dim)
-                nm, total = res[k, 0], res[k, 1]
-                models.append(Model(ang, sc, tr, float(nm / total), float(res[k, 2]), float(res[k, 3]),
-                                    float(res[k, 4]), (st.c1, st.c2, p.s, st.dim)))
+                row = rows_l[k]
+                ang = (np.float64(float(row // (L * L)) * vg.LATTICE_STEP),
+                       np.float64(float((row // L) % L) * vg.LATTICE_STEP),
+                       np.float64(float(row % L) * vg.LATTICE_STEP))
+                sc = float(score_l[k] * scale * rd3)
+                tr = vg.unravel(lin_l[k], st.dim)
+                rr = res_l[k]
+                models.append(Model(ang, sc, tr, float(np.float64(rr[0]) / rr[1]), rr[2], rr[3], rr[4],
+                                    (st.c1, st.c2, p.s, st.dim)))
             self.launches += st.launches
             out.append(AlignResult(st.dim, std_s, ave_s, top_list, models, st.launches))
         self.last_fields = [{"tdata": st.tdata, "tvec": st.tvec, "qdata": st.qdata, "qvec": st.qvec,
@@ -738,6 +752,14 @@ class Aligner:
         self._mark("end")
         self._close_marks()
         return out
+
+    def _angle_tuples(self, A, angle_comb):
+        """The rows of the angle grid of step A as tuples (cached per step)."""
+        cache = self.__dict__.setdefault("_angle_tuple_cache", {})
+        t = cache.get(float(A))
+        if t is None or len(t) != len(angle_comb):
+            t = cache[float(A)] = [tuple(r) for r in angle_comb]
+        return t
 
     def _fetch(self, groups):
         """Device tensors (a list of lists) to numpy with one copy and one

@@ -40,6 +40,56 @@ __global__ void k_prepare(float *data, int sx, int sy, int sz, float th, double 
     }
 }
 
+// The same for up to kPrepMax maps in one launch: map i takes blocks
+// [first[i], first[i + 1]) and strides over its voxels with that many blocks.
+constexpr int kPrepMax = 64;
+struct PrepMap {
+    float *data;
+    unsigned long long *out;
+    double c[3];
+    int s[3];
+    float th;
+    int first;   // first block of the map; first of entry nmap = the grid size
+};
+struct PrepBatch {
+    int nmap;
+    PrepMap m[kPrepMax + 1];
+};
+
+__global__ void k_prepare_many(const __grid_constant__ PrepBatch b) {
+    int i = 0;
+    while (i + 1 < b.nmap && b.m[i + 1].first <= (int)blockIdx.x) ++i;
+    const PrepMap &m = b.m[i];
+    const int sy = m.s[1], sz = m.s[2];
+    const size_t n = (size_t)m.s[0] * sy * sz;
+    const size_t nthr = (size_t)(b.m[i + 1].first - m.first) * blockDim.x;
+    double best = -1.0;
+    unsigned long long cnt = 0;
+    for (size_t e = (size_t)(blockIdx.x - m.first) * blockDim.x + threadIdx.x; e < n; e += nthr) {
+        float v = m.data[e];
+        if (v < m.th) {
+            v = 0.f;
+            m.data[e] = 0.f;
+        }
+        if (v != 0.f) {
+            const int k = (int)(e % sz), j = (int)((e / sz) % sy), x = (int)(e / ((size_t)sy * sz));
+            const double a = (double)x - m.c[0], bb = (double)j - m.c[1], c = (double)k - m.c[2];
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(bb, bb)), __dmul_rn(c, c));
+            best = d2 > best ? d2 : best;
+            ++cnt;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_down_sync(0xffffffffu, best, o);
+        best = w > best ? w : best;
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0 && cnt > 0) {
+        atomicMax(&m.out[0], (unsigned long long)__double_as_longlong(best));
+        atomicAdd(&m.out[1], cnt);
+    }
+}
+
 __global__ void k_init_u64(unsigned long long *p) {
     p[0] = 0ull;
     p[1] = 0ull;
@@ -192,6 +242,42 @@ extern "C" int vesper_prepare_map(float *data, int sx, int sy, int sz, double th
     const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
     k_prepare<<<blocks, 256, 0, st>>>(data, sx, sy, sz, (float)th, cent[0], cent[1], cent[2], acc);
     VG_CHECK_LAUNCH("k_prepare");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prepare_maps(int nmap, float *const *data, const int *dims, const double *thresholds,
+                                   const double *cents, uint64_t *out, void *stream) {
+    if (nmap < 0 || (nmap > 0 && (!data || !dims || !thresholds || !cents || !out)))
+        return fail(VESPER_ERR_INVALID, "vesper_prepare_maps: bad arguments");
+    for (int i = 0; i < nmap; ++i)
+        if (!data[i] || dims[3 * i] < 1 || dims[3 * i + 1] < 1 || dims[3 * i + 2] < 1)
+            return fail(VESPER_ERR_INVALID, "vesper_prepare_maps: map %d: bad arguments", i);
+    if (nmap == 0) return VESPER_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(out, 0, (size_t)nmap * 2 * sizeof(uint64_t), st) != cudaSuccess)
+        return cuda_check("vesper_prepare_maps: clear");
+    for (int i0 = 0; i0 < nmap; i0 += kPrepMax) {
+        PrepBatch b{};
+        b.nmap = std::min(kPrepMax, nmap - i0);
+        int blocks = 0;
+        for (int k = 0; k < b.nmap; ++k) {
+            const int i = i0 + k;
+            PrepMap &m = b.m[k];
+            m.data = data[i];
+            m.out = (unsigned long long *)out + 2 * (size_t)i;
+            for (int a = 0; a < 3; ++a) {
+                m.s[a] = dims[3 * i + a];
+                m.c[a] = cents[3 * i + a];
+            }
+            m.th = (float)(thresholds[i] < 0 ? 0.0 : thresholds[i]);   // th < 0 leaves data unshifted (:73-79)
+            m.first = blocks;
+            const size_t n = (size_t)m.s[0] * m.s[1] * m.s[2];
+            blocks += (int)std::min<size_t>((n + 2047) / 2048, 1024);   // about 8 voxels per thread
+        }
+        b.m[b.nmap].first = blocks;
+        k_prepare_many<<<blocks, 256, 0, st>>>(b);
+        VG_CHECK_LAUNCH("k_prepare_many");
+    }
     return VESPER_OK;
 }
 

@@ -416,6 +416,88 @@ __global__ void __launch_bounds__(256) k_prop_score_map(const uint4 *ET, const u
     }
 }
 
+// The same scores with the query's features staged in shared memory: block
+// (pair p, chunk c) scores rotations [c kScChunk, (c + 1) kScChunk) of pair p,
+// so each rotation's gathers are shared-memory loads instead of scattered L1
+// lines, and the blocks of one chunk (consecutive in launch order, pair index
+// fastest) read that chunk of the gather map while it is in L2.  Row n of the
+// staged features is zero and stands for "no source voxel" (the product of a
+// finite feature with +0 adds nothing).  Thread t sums voxels t, t + 256, ...
+// in the order of k_prop_score_map and the reduction is the same, so the scores
+// are bit-identical to it.  Pair p reads ET + p pstride and EQ + p pstride
+// (uint4 units) and writes scores + p nrot.
+constexpr int kScChunk = 32;
+constexpr int kScRPB = 8;
+template <int K8>
+__global__ void __launch_bounds__(256) k_prop_score_map_s(const uint4 *ET, const uint4 *EQ, size_t pstride,
+                                                          int npair, int d, const int16_t *srcmap, int nrot,
+                                                          float *scores) {
+    extern __shared__ uint4 sq[];   // [n + 1][K8]
+    __shared__ float red[kScRPB][8];
+    const int n = d * d * d;
+    const int p = blockIdx.x % npair, c = blockIdx.x / npair;
+    const uint4 *et = ET + (size_t)p * pstride, *eq = EQ + (size_t)p * pstride;
+    for (int e = threadIdx.x; e < n * K8; e += blockDim.x) sq[e] = __ldg(eq + e);
+    if (threadIdx.x < K8) sq[(size_t)n * K8 + threadIdx.x] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rend = min(nrot, (c + 1) * kScChunk);
+    for (int r0 = c * kScChunk; r0 < rend; r0 += kScRPB) {
+        float acc[kScRPB];
+#pragma unroll
+        for (int j = 0; j < kScRPB; ++j) acc[j] = 0.f;
+        for (int v = threadIdx.x; v < n; v += blockDim.x) {
+            int sj[kScRPB];
+#pragma unroll
+            for (int j = 0; j < kScRPB; ++j) {
+                const int s = r0 + j < rend ? (int)__ldg(srcmap + (size_t)(r0 + j) * n + v) : -1;
+                sj[j] = s < 0 ? n : s;
+            }
+            float2 t[K8][4];
+#pragma unroll
+            for (int g = 0; g < K8; ++g) {
+                const uint4 a = __ldg(et + (size_t)v * K8 + g);
+                t[g][0] = __half22float2(*(const __half2 *)&a.x);
+                t[g][1] = __half22float2(*(const __half2 *)&a.y);
+                t[g][2] = __half22float2(*(const __half2 *)&a.z);
+                t[g][3] = __half22float2(*(const __half2 *)&a.w);
+            }
+#pragma unroll
+            for (int j = 0; j < kScRPB; ++j) {
+#pragma unroll
+                for (int g = 0; g < K8; ++g) {
+                    const uint4 b = sq[(size_t)sj[j] * K8 + g];
+                    const float2 q0 = __half22float2(*(const __half2 *)&b.x), q1 = __half22float2(*(const __half2 *)&b.y);
+                    const float2 q2 = __half22float2(*(const __half2 *)&b.z), q3 = __half22float2(*(const __half2 *)&b.w);
+                    float a = acc[j];
+                    a = fmaf(t[g][0].x, q0.x, a);
+                    a = fmaf(t[g][0].y, q0.y, a);
+                    a = fmaf(t[g][1].x, q1.x, a);
+                    a = fmaf(t[g][1].y, q1.y, a);
+                    a = fmaf(t[g][2].x, q2.x, a);
+                    a = fmaf(t[g][2].y, q2.y, a);
+                    a = fmaf(t[g][3].x, q3.x, a);
+                    a = fmaf(t[g][3].y, q3.y, a);
+                    acc[j] = a;
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kScRPB; ++j) {
+            float a = acc[j];
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) red[j][warp] = a;
+        }
+        __syncthreads();
+        if (threadIdx.x < kScRPB && r0 + (int)threadIdx.x < rend) {
+            float t = 0.f;
+            for (int w = 0; w < 8; ++w) t += red[threadIdx.x][w];
+            scores[(size_t)p * nrot + r0 + threadIdx.x] = t;
+        }
+        __syncthreads();   // red is rewritten by the next group
+    }
+}
+
 // Partial gradients of the correlation for channels [k0, k0 + kc): block b
 // takes rotations [b*chunk, (b+1)*chunk) and writes part[b][0][k][v] =
 // sum_r g_r EQ[k][src_r(v)] and part[b][1][k][s] = sum_r g_r ET[k][v] summed
@@ -774,6 +856,31 @@ extern "C" int vesper_prop_srcmap(int d, const float *rotmats, int nrot, void *s
     return VESPER_OK;
 }
 
+// launch of k_prop_score_map_s for npair pairs, or false when the query's
+// features do not fit in shared memory
+static bool score_map_staged(const uint4 *et, const uint4 *eq, size_t pstride, int npair, int K8, int d,
+                             const int16_t *m, int nrot, float *scores, cudaStream_t st) {
+    const int n = d * d * d;
+    const size_t sm = ((size_t)n + 1) * K8 * sizeof(uint4);
+    if (sm > (size_t)smem_limit()) return false;
+    const unsigned nb = (unsigned)(npair * ((nrot + kScChunk - 1) / kScChunk));
+    switch (K8) {
+        case 1:
+            allow_smem(k_prop_score_map_s<1>, sm);
+            k_prop_score_map_s<1><<<nb, 256, sm, st>>>(et, eq, pstride, npair, d, m, nrot, scores);
+            return true;
+        case 2:
+            allow_smem(k_prop_score_map_s<2>, sm);
+            k_prop_score_map_s<2><<<nb, 256, sm, st>>>(et, eq, pstride, npair, d, m, nrot, scores);
+            return true;
+        case 4:
+            allow_smem(k_prop_score_map_s<4>, sm);
+            k_prop_score_map_s<4><<<nb, 256, sm, st>>>(et, eq, pstride, npair, d, m, nrot, scores);
+            return true;
+    }
+    return false;
+}
+
 extern "C" int vesper_prop_score_map(const void *ET, const void *EQ, int K, int d, const void *srcmap, int nrot,
                                      float *scores, void *stream) {
     if (!ET || !EQ || !srcmap || !scores || d < 1 || nrot < 0 || K < 8 || K % 8 || K > 32)
@@ -781,10 +888,14 @@ extern "C" int vesper_prop_score_map(const void *ET, const void *EQ, int K, int 
     if (((uintptr_t)ET | (uintptr_t)EQ) & 15) return fail(VESPER_ERR_INVALID, "prop_score_map: 16-byte alignment");
     if (nrot == 0) return VESPER_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    constexpr int RPB = 4;
-    const unsigned nb = (unsigned)((nrot + RPB - 1) / RPB);
     const uint4 *a = (const uint4 *)ET, *b = (const uint4 *)EQ;
     const int16_t *m = (const int16_t *)srcmap;
+    if (score_map_staged(a, b, 0, 1, K / 8, d, m, nrot, scores, st)) {
+        VG_CHECK_LAUNCH("k_prop_score_map_s");
+        return VESPER_OK;
+    }
+    constexpr int RPB = 4;
+    const unsigned nb = (unsigned)((nrot + RPB - 1) / RPB);
     switch (K / 8) {
         case 1: k_prop_score_map<1, RPB><<<nb, 256, 0, st>>>(a, b, d, m, nrot, scores); break;
         case 2: k_prop_score_map<2, RPB><<<nb, 256, 0, st>>>(a, b, d, m, nrot, scores); break;
@@ -792,6 +903,29 @@ extern "C" int vesper_prop_score_map(const void *ET, const void *EQ, int K, int 
         default: return fail(VESPER_ERR_UNSUPPORTED, "prop_score_map: K = %d", K);
     }
     VG_CHECK_LAUNCH("k_prop_score_map");
+    return VESPER_OK;
+}
+
+extern "C" int vesper_prop_score_map_many(const void *VM, int npair, int K, int d, const void *srcmap, int nrot,
+                                          float *scores, void *stream) {
+    if (!VM || !srcmap || !scores || npair < 0 || d < 1 || nrot < 0 || K < 8 || K % 8 || K > 32)
+        return fail(VESPER_ERR_INVALID, "prop_score_map_many: bad args (K a multiple of 8, <= 32)");
+    if ((uintptr_t)VM & 15) return fail(VESPER_ERR_INVALID, "prop_score_map_many: 16-byte alignment");
+    if (npair == 0 || nrot == 0) return VESPER_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int K8 = K / 8;
+    const size_t per = (size_t)d * d * d * K8;   // uint4 per map
+    const uint4 *vm = (const uint4 *)VM;
+    const int16_t *m = (const int16_t *)srcmap;
+    if (score_map_staged(vm, vm + per, 2 * per, npair, K8, d, m, nrot, scores, st)) {
+        VG_CHECK_LAUNCH("k_prop_score_map_s");
+        return VESPER_OK;
+    }
+    for (int i = 0; i < npair; ++i) {
+        const int rc = vesper_prop_score_map(vm + 2 * i * per, vm + (2 * i + 1) * per, K, d, srcmap, nrot,
+                                             scores + (size_t)i * nrot, stream);
+        if (rc != VESPER_OK) return rc;
+    }
     return VESPER_OK;
 }
 

@@ -38,7 +38,6 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
-#include <map>
 #include <mutex>
 #include <type_traits>
 
@@ -65,25 +64,35 @@ struct TcGeom {
     static constexpr size_t SMEM = 2 * B_BYTES + 2 * A_BYTES + STAGE_BYTES + 64 + 4096;
 };
 
-// The real-form DFT matrix, hi then lo, in the K-major core-matrix layout.
+// The real-form DFT matrix, hi then lo, in the K-major core-matrix layout,
+// written into shared memory by every CTA (no table in device memory).  Entry
+// (n, k) is c, s, -s or c of the angle 2 pi m / D, m = (n/2)(k/2) mod D, so the
+// D cosines and sines are computed once (float64 sincospi, then split into
+// bf16 hi + lo of the float64 value) and the K^2 entries looked up.
 template <int D>
-__global__ void k_tc_table(unsigned char *tab) {
+__device__ void tc_build_table(unsigned char *bh, unsigned char *bl, __nv_bfloat16 (*tw)[D], int tid, int nthr) {
     constexpr int K = TcGeom<D>::K;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= K * K) return;
-    const int n = i / K, k = i % K;
-    const int kk = n >> 1, x = k >> 1;
-    const int m = (kk * x) % D;
-    double s, c;
-    sincospi(2.0 * (double)m / (double)D, &s, &c);
-    double v;
-    if ((n & 1) == 0) v = (k & 1) == 0 ? c : s;
-    else v = (k & 1) == 0 ? -s : c;
-    const __nv_bfloat16 hi = __double2bfloat16(v);
-    const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(hi));
-    const uint32_t off = tc::kmajor_off(n, k, K);
-    *(__nv_bfloat16 *)(tab + off) = hi;
-    *(__nv_bfloat16 *)(tab + TcGeom<D>::B_BYTES + off) = lo;
+    for (int m = tid; m < D; m += nthr) {
+        double s, c;
+        sincospi(2.0 * (double)m / (double)D, &s, &c);
+        const double v[3] = {c, s, -s};
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            const __nv_bfloat16 hi = __double2bfloat16(v[e]);
+            tw[2 * e][m] = hi;
+            tw[2 * e + 1][m] = __double2bfloat16(v[e] - (double)__bfloat162float(hi));
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < K * K; i += nthr) {
+        const int n = i / K, k = i % K;
+        const int m = ((n >> 1) * (k >> 1)) % D;
+        // c, s for even rows; -s, c for odd rows
+        const int e = (n & 1) == 0 ? ((k & 1) == 0 ? 0 : 1) : ((k & 1) == 0 ? 2 : 0);
+        const uint32_t off = tc::kmajor_off(n, k, K);
+        *(__nv_bfloat16 *)(bh + off) = tw[2 * e][m];
+        *(__nv_bfloat16 *)(bl + off) = tw[2 * e + 1][m];
+    }
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) {
@@ -137,7 +146,7 @@ __device__ __forceinline__ void issue_split_mma(uint32_t tmem, const unsigned ch
 
 template <int D>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_tcb(const PassB2 a, const unsigned char *tab, const __grid_constant__ CUtensorMap tmS, int *err, int stall,
+    k_tcb(const PassB2 a, const __grid_constant__ CUtensorMap tmS, int *err, int stall,
           uint64_t limit_ns) {
     using G = TcGeom<D>;
     constexpr int K = G::K;
@@ -159,9 +168,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
     // the DFT matrix (hi, lo) into shared memory
     {
-        const uint4 *src = (const uint4 *)tab;
-        uint4 *dst = (uint4 *)smem;
-        for (int i = tid; i < (int)(2 * G::B_BYTES / 16); i += kTcThreads) dst[i] = __ldg(src + i);
+        __shared__ __nv_bfloat16 tw[6][D];
+        tc_build_table<D>(bh, bl, tw, tid, kTcThreads);
     }
     if (tid == 0) {
         tc::mbar_init(mbar_mma, 1);
@@ -297,28 +305,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 // ---- host ---------------------------------------------------------------------
 
-// the DFT table of side D on the current device, built on first use
-template <int D>
-static const unsigned char *tc_table(cudaStream_t st) {
-    static std::mutex mu;
-    static std::map<int, unsigned char *> tabs;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> g(mu);
-    auto it = tabs.find(dev);
-    if (it != tabs.end()) return it->second;
-    unsigned char *p = nullptr;
-    if (cudaMalloc(&p, 2 * TcGeom<D>::B_BYTES) != cudaSuccess) return nullptr;
-    constexpr int n = TcGeom<D>::K * TcGeom<D>::K;
-    k_tc_table<D><<<(n + 255) / 256, 256, 0, st>>>(p);
-    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
-        cudaFree(p);
-        return nullptr;
-    }
-    tabs[dev] = p;
-    return p;
-}
-
 bool tc_pass_b_supported(int d) { return d == 32 || d == 64; }
 
 // rotations per full wave of pass-B CTAs on this device (column tiles of 128
@@ -370,16 +356,13 @@ int tc_pass_b(const PassB2 &a, int nb, int *err, cudaStream_t st, int stall, uin
     if (nb < 1 || nb > 65535 || !err) return fail(VESPER_ERR_INVALID, "tc pass B: bad batch");
     auto run = [&](auto dc) -> int {
         constexpr int D = decltype(dc)::value;
-        const unsigned char *tab = tc_table<D>(st);
-        if (!tab) return cuda_check("tc pass B: DFT table");
         constexpr size_t sm = TcGeom<D>::SMEM;
         allow_smem(k_tcb<D>, sm);
         const int dH = D * (D / 2 + 1);
         CUtensorMap tmS;
         if ((dH * 8) % 16 || !box_map(&tmS, a.S, D, dH, nb * a.nch))
             return fail(VESPER_ERR_CUDA, "tc pass B: tensor map (driver entry point or alignment)");
-        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcThreads, sm, st>>>(a, tab, tmS, err, stall,
-                                                                                 limit_ns);
+        k_tcb<D><<<dim3((dH + kTcRows - 1) / kTcRows, nb), kTcThreads, sm, st>>>(a, tmS, err, stall, limit_ns);
         VG_CHECK_LAUNCH("k_tcb");
         return VESPER_OK;
     };

@@ -168,7 +168,8 @@ class ProposalNet:
         """Inference for P pairs of one pooled side at once: fields
         [2P][4][d][d][d] (target and query of pair i at 2i, 2i + 1) -> scores
         [P][nrot], with one encoder launch per layer and one voxel-major
-        conversion for all 2P maps, then one scoring launch per pair."""
+        conversion for all 2P maps, then one scoring launch for every pair
+        (one per pair when the gather map is not cached)."""
         d = int(fTQ.shape[-1])
         nm = int(fTQ.shape[0])
         npair = nm // 2
@@ -180,11 +181,11 @@ class ProposalNet:
             vm = torch.empty((nm, d * d * d, K), dtype=torch.float16, device=self.dev.device)
             _native.check(self.lib.vesper_prop_vmajor_f16(_p(feat), K, d, nm, _p(vm), self.dev.stream))
             sm = srcmap(self.dev, d, mats)
-            for i in range(npair):
-                if sm is not None:
-                    _native.check(self.lib.vesper_prop_score_map(_p(vm[2 * i]), _p(vm[2 * i + 1]), K, d, _p(sm), n,
-                                                                 _p(s[i]), self.dev.stream))
-                else:
+            if sm is not None:     # every pair in one launch
+                _native.check(self.lib.vesper_prop_score_map_many(_p(vm), npair, K, d, _p(sm), n, _p(s),
+                                                                  self.dev.stream))
+            else:
+                for i in range(npair):
                     _native.check(self.lib.vesper_prop_score_f16(_p(vm[2 * i]), _p(vm[2 * i + 1]), K, d, _p(mats), n,
                                                                  _p(s[i]), self.dev.stream))
         else:
