@@ -1,9 +1,10 @@
 """Small, self-contained cases for profiler captures of single kernels, run
 through ``python bench.py --case <name> [arg]``:
 
-  search<d> [nrot]
+  search<d> [nrot [batch]]
       three register/fused-path searches of seeded random side-d fields over
-      the first nrot (default 1008) rotations of the 30-degree grid
+      the first nrot (default 1008) rotations of the 30-degree grid, with the
+      autotuned launch shape or the given batch
   prop
       learned-proposal scorings (committed weights) of one held-out
       128^3 / 64^3 pair at s = 3 over the 10-degree grid, timed
@@ -51,8 +52,9 @@ def main(argv=None):
         td, tv = dev.to_dev(data), dev.to_dev(vec.astype(np.float32))
         spec = vg.target_spectra_device(td, tv, "VecProduct", 0.0, dev=dev)
         mats = dev.to_dev(vg.rot_matrices(vg.calc_angle_comb(30.0)[:nrot]))
+        batch = int(argv[2]) if len(argv) > 2 else 0     # a fixed batch: no autotuning launches
         for _ in range(3):
-            vg.search_device(spec, td, tv, "VecProduct", 0.0, mats, dev=dev, tuned=True)
+            vg.search_device(spec, td, tv, "VecProduct", 0.0, mats, dev=dev, tuned=batch == 0, batch=batch)
     elif what.startswith("prob"):
         # prob mode: both passes (statistics pass, mixed pass) over the 15-degree
         # grid on seeded random side-d fields with four probability channels;

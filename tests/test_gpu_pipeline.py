@@ -305,3 +305,26 @@ def test_prepare_maps_equals_per_map(dev):
         np.testing.assert_array_equal(got[i], ref_out[i], err_msg=f"map {i}")
         np.testing.assert_array_equal(ts[i].cpu().numpy(), ref_data[i], err_msg=f"map {i}")
     assert got[3, 1] == 0 and got[3, 0] == 0
+
+
+def test_graph_late_stage_many_pairs_of_one_side(dev):
+    """Eight 128^3 / 64^3 pairs whose grids share sides (28 to 32, the
+    three-pass search): the graph form runs the pairs' refinement chains on
+    concurrent streams, and every pair's results equal the eager form's (no
+    scratch is shared between streams)."""
+    from vesper_python_gb300 import align, synth
+    al = align.Aligner(dev)
+    p = align.AlignParams(t=0.1, T=0.1, g=16.0, s=3.0, A=30.0, N=5, mode="VecProduct")
+    pairs = [synth.workload_pair("prop128_s3_a10", seed=s) for s in range(8)]
+    items = [(dev.to_dev(pr.map1), dev.to_dev(pr.map2), pr.width, pr.width, pr.orig1, pr.orig2) for pr in pairs]
+    eager = al.align_many(items, p)
+    dims = [r.dim for r in eager]
+    assert len(set(dims)) < len(dims) and min(dims) > 24
+    for _ in range(2):
+        g = al.align_many(items, p, graph=True)
+        for a, r in zip(eager, g):
+            assert r.top == a.top
+            assert [m.angle for m in r.models] == [m.angle for m in a.models]
+            assert [m.vec_trans for m in r.models] == [m.vec_trans for m in a.models]
+            assert [m.dot_score for m in r.models] == [m.dot_score for m in a.models]
+            assert [m.cc for m in r.models] == [m.cc for m in a.models]

@@ -283,8 +283,11 @@ class Aligner:
             # host value in between, replayed as one CUDA graph.  (Eager calls
             # keep the host-driven refinement below, which searches each
             # distinct angle once: fewer rotations, one more host round trip.)
+            # the global results go to the host while the refinement runs
+            gh = self._fetch_start([[st.scores[:, 0].contiguous(), st.lin[:, 0].contiguous(), st.top] +
+                                    ([st.order] if st.order is not None else []) for st in P], slot=0)
             self._late_stage_graph(P, p, stats, mats)
-            return self._finish_device_late(P, p, stats, angle_comb, nang)
+            return self._finish_device_late(P, p, gh, angle_comb)
         if sh is None:
             sh = stats.cpu().numpy()
             self.d2h_bytes += sh.nbytes
@@ -625,38 +628,51 @@ class Aligner:
         nscore = dev.lib.vesper_search_nscore(vg.MODE_CODES[mode], 0)
         RS = torch.empty((n, N * 27, nscore), dtype=torch.float32, device=dev.device)
         RL = torch.empty((n, N * 27, nscore), dtype=torch.int32, device=dev.device)
-        for i, st in enumerate(P):
-            vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats[i], batch=p.batch, dev=dev, tuned=True,
-                             out=(RS[i], RL[i]))
-            st.launches += self._search_launches(st.dim, mode, N * 27, p.batch)
-        masked = torch.where(valid, RS[:, :, 0], torch.full_like(RS[:, :, 0], float("-inf")))
-        rtop = torch.stack([vg.topn_device(masked[i].contiguous(), N, dev=dev) for i in range(n)])   # [n, N]
-        sel = rtop.to(torch.int64).clamp(min=0)
-        r_rows = crow.gather(1, sel)
-        r_score = RS[:, :, 0].gather(1, sel)
-        r_lin = RL[:, :, 0].to(torch.int64).gather(1, sel)
-        mm = lat.index_select(0, r_rows.reshape(-1)).reshape(n, N, 3, 3)
-        self._mark("rescore")
+        # every pair's chain (search of its slots, top-N, gather and float64
+        # rescoring of the refined models) on one of FV_STREAMS side streams:
+        # the chains are short launches that fill little of the GPU, so pairs
+        # overlap; the streams fork from and join the current stream (also
+        # inside a CUDA-graph capture).  The shared inputs above are freed only
+        # after the join.
+        cur = torch.cuda.current_stream(dev.device)
+        capturing = torch.cuda.is_current_stream_capturing()
+        side = self._side_streams()
+        for sd in side:
+            sd.wait_stream(cur)
         for i, st in enumerate(P):
             d = st.dim
-            st.launches += 1
-            st.rtop, st.r_rows, st.r_score, st.r_lin = rtop[i], r_rows[i], r_score[i], r_lin[i]
-            gd, gv, _ = vg.rot_gather_device(st.qdata, st.qvec, mm[i], dev=dev)
-            lin = r_lin[i]
-            t = torch.stack([lin // (d * d), (lin // d) % d, lin % d], dim=1)
-            trd = torch.where(2 * t > d, t - d, t).to(torch.int32).contiguous()   # wrapped as get_score (:1323-1329)
-            st.res = torch.empty((N, 8), dtype=torch.float64, device=dev.device)
-            ws = dev.workspace(("rescore_batch", i, d, N), _native.size_query("vesper_rescore_batch_workspace_size", d, N))
-            _native.check(self.lib.vesper_rescore_batch_dev(
-                ctypes.c_void_p(st.tdata.data_ptr()), ctypes.c_void_p(st.tvec.data_ptr()),
-                ctypes.c_void_p(stats[i].data_ptr()), ctypes.c_void_p(gd.data_ptr()), ctypes.c_void_p(gv.data_ptr()),
-                d, ctypes.c_void_p(trd.data_ptr()), N, ctypes.c_void_p(st.res.data_ptr()),
-                ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
-            st.launches += 5
-            if self.pair_events is not None and not torch.cuda.is_current_stream_capturing():
-                e = torch.cuda.Event(enable_timing=True)
-                e.record()
-                self.pair_events.append(e)
+            with torch.cuda.stream(side[i % len(side)]):
+                vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats[i], batch=p.batch, dev=dev,
+                                 tuned=True, out=(RS[i], RL[i]))
+                masked = torch.where(valid[i], RS[i, :, 0], torch.full_like(RS[i, :, 0], float("-inf")))
+                rtop = vg.topn_device(masked.contiguous(), N, dev=dev)
+                sel = rtop.to(torch.int64).clamp(min=0)
+                st.rtop, st.r_rows = rtop, crow[i].gather(0, sel)
+                st.r_score = RS[i, :, 0].gather(0, sel)
+                st.r_lin = RL[i, :, 0].to(torch.int64).gather(0, sel)
+                mm = lat.index_select(0, st.r_rows)
+                gd, gv, _ = vg.rot_gather_device(st.qdata, st.qvec, mm, dev=dev)
+                lin = st.r_lin
+                t = torch.stack([lin // (d * d), (lin // d) % d, lin % d], dim=1)
+                trd = torch.where(2 * t > d, t - d, t).to(torch.int32).contiguous()   # wrapped as get_score (:1323-1329)
+                st.res = torch.empty((N, 8), dtype=torch.float64, device=dev.device)
+                ws = dev.workspace(("rescore_batch", i, d, N),
+                                   _native.size_query("vesper_rescore_batch_workspace_size", d, N))
+                _native.check(self.lib.vesper_rescore_batch_dev(
+                    ctypes.c_void_p(st.tdata.data_ptr()), ctypes.c_void_p(st.tvec.data_ptr()),
+                    ctypes.c_void_p(stats[i].data_ptr()), ctypes.c_void_p(gd.data_ptr()),
+                    ctypes.c_void_p(gv.data_ptr()), d, ctypes.c_void_p(trd.data_ptr()), N,
+                    ctypes.c_void_p(st.res.data_ptr()), ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
+                if self.pair_events is not None and not capturing:
+                    e = torch.cuda.Event(enable_timing=True)
+                    e.record()
+                    self.pair_events.append(e)
+            st.launches += self._search_launches(d, mode, N * 27, p.batch) + 7
+            if not capturing:
+                for tt in (st.rtop, st.r_rows, st.r_score, st.r_lin, st.res):
+                    tt.record_stream(cur)    # made on a side stream, read on this one
+        for sd in side:
+            cur.wait_stream(sd)
 
     _LATE_FIELDS = ("rtop", "r_rows", "r_score", "r_lin", "res", "launches")
 
@@ -700,30 +716,25 @@ class Aligner:
             self.pair_events.extend([e] * len(P))
         self.graph_replays += 1
 
-    def _finish_device_late(self, P, p, stats, angle_comb, nang):
-        """One wait for every pair's global and refined results, then the host
-        bookkeeping: statistics and top-N list of the global pass, refined
-        models and their scores."""
+    def _finish_device_late(self, P, p, gh, angle_comb):
+        """The host bookkeeping of the device late stage: the global pass's
+        statistics and top-N list from the results ``gh`` (copied before the
+        late stage was launched, so this part runs while the device refines),
+        then one wait for the refined models and their scores.  Modes CC and
+        PCC never come here, so every score scale is 1."""
         mode = p.mode
+        assert mode not in ("CC", "PCC")
         L = vg.LATTICE_N
         self._mark("results")
-        groups = [[st.scores[:, 0].contiguous(), st.lin[:, 0].contiguous(), st.top,
-                   st.rtop, st.r_rows, st.r_score, st.r_lin, st.res] +
-                  ([st.order] if st.order is not None else []) for st in P]
-        groups.append([stats])
-        h = self._fetch(groups)
-        sh = h[-1][0]
-        out = []
+        late = self._fetch_start([[st.rtop, st.r_rows, st.r_score, st.r_lin, st.res] for st in P], slot=1)
+        glob = self._fetch_finish(gh)
         angles = self._angle_tuples(p.A, angle_comb)
+        scale = 1.0
+        head = []
         for i, st in enumerate(P):
-            raw, lin_h, top, rtop, r_rows, r_score, r_lin, res = h[i][:8]
-            order = h[i][8] if st.order is not None else None
+            raw, lin_h, top = glob[i][:3]
+            order = glob[i][3] if st.order is not None else None
             rd3 = 1.0 / st.dim ** 3
-            scale = 1.0
-            if mode == "CC":
-                scale = 1.0 / sh[i, 3] ** 2
-            elif mode == "PCC":
-                scale = 1.0 / sh[i, 4] ** 2
             tpos = [t for t in top.tolist() if t >= 0]      # positions in the searched rotations
             top_h = [int(order[t]) for t in tpos] if order is not None else tpos   # -> grid indices
             score_arr = raw.astype(np.float64) * scale * rd3
@@ -731,6 +742,12 @@ class Aligner:
             # the score of grid index order[t] is that of position t (float32 -> float64, * scale * rd3)
             top_list = [(angles[r], float(np.float64(raw[t]) * scale * rd3), vg.unravel(lin_h[t], st.dim))
                         for t, r in zip(tpos, top_h)]
+            head.append((ave_s, std_s, top_list))
+        h = self._fetch_finish(late)
+        out = []
+        for i, st in enumerate(P):
+            rtop, r_rows, r_score, r_lin, res = h[i]
+            rd3 = 1.0 / st.dim ** 3
             models = []
             rows_l, score_l, lin_l, res_l = r_rows.tolist(), r_score.tolist(), r_lin.tolist(), res.tolist()
             for k, rk in enumerate(rtop.tolist()):
@@ -746,6 +763,7 @@ class Aligner:
                 models.append(Model(ang, sc, tr, float(np.float64(rr[0]) / rr[1]), rr[2], rr[3], rr[4],
                                     (st.c1, st.c2, p.s, st.dim)))
             self.launches += st.launches
+            ave_s, std_s, top_list = head[i]
             out.append(AlignResult(st.dim, std_s, ave_s, top_list, models, st.launches))
         self.last_fields = [{"tdata": st.tdata, "tvec": st.tvec, "qdata": st.qdata, "qvec": st.qvec,
                              "ave": float(st.ave)} for st in P]
@@ -760,6 +778,34 @@ class Aligner:
         if t is None or len(t) != len(angle_comb):
             t = cache[float(A)] = [tuple(r) for r in angle_comb]
         return t
+
+    def _fetch_start(self, groups, slot):
+        """Start the copy of device tensors (a list of lists) to the host: one
+        packed transfer into pinned buffer ``slot`` (one per copy that can be
+        in flight), ordered on the current stream; _fetch_finish waits for it
+        and returns the numpy arrays."""
+        packed, layout = pack_bytes([t for g in groups for t in g])
+        lens = [len(g) for g in groups]
+        if packed is None:
+            return None, layout, None, lens
+        bufs = self.__dict__.setdefault("_pinned_slots", {})
+        host = bufs.get(slot)
+        if host is None or host.numel() < packed.numel():
+            host = bufs[slot] = torch.empty(max(packed.numel(), 1 << 20), dtype=torch.uint8, pin_memory=True)
+        host[:packed.numel()].copy_(packed, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        self.d2h_bytes += packed.numel()
+        return host, layout, ev, lens
+
+    @staticmethod
+    def _fetch_finish(handle):
+        host, layout, ev, lens = handle
+        if host is None:
+            return [[] for _ in lens]
+        ev.synchronize()
+        arrays = iter(unpack_bytes(host.numpy(), layout))
+        return [[next(arrays) for _ in range(k)] for k in lens]
 
     def _fetch(self, groups):
         """Device tensors (a list of lists) to numpy with one copy and one

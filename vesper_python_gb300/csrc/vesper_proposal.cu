@@ -49,20 +49,25 @@ __global__ void k_conv_fwd(const float *in, int cin, const __nv_bfloat16 *W, con
 
 // The same layer with COG output channels per thread: one input load feeds
 // COG products, the block's COG x cin x 27 weights sit in shared memory as
-// float32 (every thread reads the same weight at the same step: a broadcast),
-// and the 27 neighbour offsets and their in-grid mask are computed once per
-// voxel.  The summation order per output is that of k_conv_fwd (bias, then
-// ci, then tap), so the results are the same bits.
+// float32 in [cin][27][COG] order (every thread reads the same COG weights at
+// the same step: one 16-byte broadcast load per four), and the 27 neighbour
+// offsets and their in-grid mask are computed once per voxel.  The summation
+// order per output is that of k_conv_fwd (bias, then ci, then tap), so the
+// results are the same bits.
 template <int COG>
 __global__ void __launch_bounds__(128) k_conv_fwd_g(const float *in, int cin, const __nv_bfloat16 *W,
                                                     const float *bias, int cout, int d, int relu, float *out) {
-    extern __shared__ float wsh[];   // [COG][cin][27]
+    static_assert(COG % 4 == 0, "COG: a multiple of 4");
+    extern __shared__ float4 wsh4[];   // [cin][27][COG / 4]
+    float *wsh = (float *)wsh4;
     const int n = d * d * d;
     const int co0 = blockIdx.y * COG;
     in += (size_t)blockIdx.z * cin * n;
     out += (size_t)blockIdx.z * cout * n;
-    for (int i = threadIdx.x; i < COG * cin * 27; i += blockDim.x)
-        wsh[i] = __bfloat162float(W[(size_t)co0 * cin * 27 + i]);
+    for (int i = threadIdx.x; i < COG * cin * 27; i += blockDim.x) {
+        const int j = i / (cin * 27), t = i - j * cin * 27;   // t = ci * 27 + o
+        wsh[t * COG + j] = __bfloat162float(W[(size_t)co0 * cin * 27 + i]);
+    }
     __syncthreads();
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
@@ -78,13 +83,19 @@ __global__ void __launch_bounds__(128) k_conv_fwd_g(const float *in, int cin, co
     for (int j = 0; j < COG; ++j) acc[j] = bias ? bias[co0 + j] : 0.f;
     for (int ci = 0; ci < cin; ++ci) {
         const float *src = in + (size_t)ci * n + v;
-        const float *w = wsh + ci * 27;
+        const float4 *w = wsh4 + (size_t)ci * 27 * (COG / 4);
 #pragma unroll
         for (int o = 0; o < 27; ++o) {
             if (!(mask & (1u << o))) continue;
             const float val = src[((o / 9 - 1) * d + ((o / 3) % 3 - 1)) * d + (o % 3 - 1)];
 #pragma unroll
-            for (int j = 0; j < COG; ++j) acc[j] = fmaf(w[j * cin * 27 + o], val, acc[j]);
+            for (int q = 0; q < COG / 4; ++q) {
+                const float4 w4 = w[o * (COG / 4) + q];
+                acc[4 * q + 0] = fmaf(w4.x, val, acc[4 * q + 0]);
+                acc[4 * q + 1] = fmaf(w4.y, val, acc[4 * q + 1]);
+                acc[4 * q + 2] = fmaf(w4.z, val, acc[4 * q + 2]);
+                acc[4 * q + 3] = fmaf(w4.w, val, acc[4 * q + 3]);
+            }
         }
     }
 #pragma unroll
@@ -746,11 +757,17 @@ extern "C" int vesper_prop_conv_fwd(const float *in, int cin, const void *W, con
     if (!in || !W || !out || cin < 1 || cout < 1 || d < 1 || nmap < 1 || nmap > 65535)
         return fail(VESPER_ERR_INVALID, "conv_fwd: bad args");
     const int n = d * d * d;
-    constexpr int COG = 4;
-    const size_t sm = (size_t)COG * cin * 27 * sizeof(float);
-    if (cout % COG == 0 && sm <= (size_t)smem_limit()) {
-        allow_smem(k_conv_fwd_g<COG>, sm);
-        k_conv_fwd_g<COG><<<dim3((n + 127) / 128, cout / COG, nmap), 128, sm, (cudaStream_t)stream>>>(
+    // 8 output channels per thread where they divide cout, else 4
+    const size_t sm8 = (size_t)8 * cin * 27 * sizeof(float), sm4 = (size_t)4 * cin * 27 * sizeof(float);
+    if (cout % 8 == 0 && sm8 <= (size_t)smem_limit()) {
+        allow_smem(k_conv_fwd_g<8>, sm8);
+        k_conv_fwd_g<8><<<dim3((n + 127) / 128, cout / 8, nmap), 128, sm8, (cudaStream_t)stream>>>(
+            in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
+        VG_CHECK_LAUNCH("k_conv_fwd_g");
+        return VESPER_OK;
+    } else if (cout % 4 == 0 && sm4 <= (size_t)smem_limit()) {
+        allow_smem(k_conv_fwd_g<4>, sm4);
+        k_conv_fwd_g<4><<<dim3((n + 127) / 128, cout / 4, nmap), 128, sm4, (cudaStream_t)stream>>>(
             in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
         VG_CHECK_LAUNCH("k_conv_fwd_g");
         return VESPER_OK;

@@ -460,15 +460,17 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
             _TUNED[tk] = t
         batch = int(t["batch"])
         opts = (-1, int(t["cchunk"]), int(t["W"]))
-    # per call shape: scores per rotation, the workspace and the options array
+    # per call shape: scores per rotation, the workspace size and the options
+    # array (the workspace itself is looked up per call: it belongs to the
+    # current stream, and searches on different streams run concurrently)
     sk = (dev.device, d, code, mix is not None, int(batch), max(n, 1), tuple(opts) if opts is not None else None)
     ent = _SEARCH_SIZES.get(sk)
     if ent is None:
         ws_bytes = _native.size_query("vesper_search_workspace_size", d, code, int(batch), max(n, 1))
-        ent = _SEARCH_SIZES[sk] = (dev.lib.vesper_search_nscore(code, 1 if mix is not None else 0),
-                                   dev.workspace(("search", d, code, int(batch)), ws_bytes),
+        ent = _SEARCH_SIZES[sk] = (dev.lib.vesper_search_nscore(code, 1 if mix is not None else 0), ws_bytes,
                                    (ctypes.c_int * 3)(*[int(v) for v in opts]) if opts is not None else None)
-    nscore, ws, copts = ent
+    nscore, ws_bytes, copts = ent
+    ws = dev.workspace(("search", d, code, int(batch)), ws_bytes)
     if out is not None:
         scores, lin = out
         if (tuple(scores.shape) != (n, nscore) or tuple(lin.shape) != (n, nscore) or not scores.is_contiguous()
