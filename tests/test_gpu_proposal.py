@@ -349,9 +349,9 @@ def test_score_map_many_matches_per_pair(dev, d, K, npair):
 
 @pytest.mark.parametrize("relu", [0, 1])
 def test_conv_forward_kernels_bit_identical(dev, relu):
-    """The encoder convolution with 8 output channels per thread (cout a
-    multiple of 8), with 4 (a multiple of 4) and with one (otherwise) sums in
-    the same order, so the same output channels come out bit for bit."""
+    """The encoder convolution with 4 output channels per thread (cout a
+    multiple of 4) and with one (otherwise) sums in the same order, so the same
+    output channels come out bit for bit."""
     import ctypes
     from vesper_python_gb300 import _native
     rng = np.random.default_rng(3 + relu)
@@ -361,11 +361,12 @@ def test_conv_forward_kernels_bit_identical(dev, relu):
     x = dev.to_dev(rng.normal(size=(nmap, cin, d, d, d)), torch.float32)
     p = lambda t: ctypes.c_void_p(t.data_ptr())
     outs = {}
-    for cout in (24, 12, 6):
+    for cout in (24, 12, 6, 3):
         o = torch.full((nmap, cout, d, d, d), float("nan"), device=dev.device)
         Wc = W[:cout].contiguous()
         _native.check(dev.lib.vesper_prop_conv_fwd(p(x), cin, p(Wc), p(b), cout, d, relu, nmap, p(o), dev.stream))
         outs[cout] = o.cpu().numpy()
     np.testing.assert_array_equal(outs[24][:, :12], outs[12])
     np.testing.assert_array_equal(outs[24][:, :6], outs[6])
+    np.testing.assert_array_equal(outs[24][:, :3], outs[3])
     assert np.isfinite(outs[24]).all()

@@ -757,17 +757,12 @@ extern "C" int vesper_prop_conv_fwd(const float *in, int cin, const void *W, con
     if (!in || !W || !out || cin < 1 || cout < 1 || d < 1 || nmap < 1 || nmap > 65535)
         return fail(VESPER_ERR_INVALID, "conv_fwd: bad args");
     const int n = d * d * d;
-    // 8 output channels per thread where they divide cout, else 4
-    const size_t sm8 = (size_t)8 * cin * 27 * sizeof(float), sm4 = (size_t)4 * cin * 27 * sizeof(float);
-    if (cout % 8 == 0 && sm8 <= (size_t)smem_limit()) {
-        allow_smem(k_conv_fwd_g<8>, sm8);
-        k_conv_fwd_g<8><<<dim3((n + 127) / 128, cout / 8, nmap), 128, sm8, (cudaStream_t)stream>>>(
-            in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
-        VG_CHECK_LAUNCH("k_conv_fwd_g");
-        return VESPER_OK;
-    } else if (cout % 4 == 0 && sm4 <= (size_t)smem_limit()) {
-        allow_smem(k_conv_fwd_g<4>, sm4);
-        k_conv_fwd_g<4><<<dim3((n + 127) / 128, cout / 4, nmap), 128, sm4, (cudaStream_t)stream>>>(
+    // 4 output channels per thread (measured: 8 per thread was 10 % slower over the encoder)
+    constexpr int COG = 4;
+    const size_t sm = (size_t)COG * cin * 27 * sizeof(float);
+    if (cout % COG == 0 && sm <= (size_t)smem_limit()) {
+        allow_smem(k_conv_fwd_g<COG>, sm);
+        k_conv_fwd_g<COG><<<dim3((n + 127) / 128, cout / COG, nmap), 128, sm, (cudaStream_t)stream>>>(
             in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
         VG_CHECK_LAUNCH("k_conv_fwd_g");
         return VESPER_OK;
