@@ -439,6 +439,22 @@ __global__ void __launch_bounds__(256) k_prop_score_map(const uint4 *ET, const u
 // (uint4 units) and writes scores + p nrot.
 constexpr int kScChunk = 32;
 constexpr int kScRPB = 8;
+
+// c + a.lo * b.lo, then + a.hi * b.hi, for packed float16 pairs a, b: each step
+// one fma.rn.f32.f16 (float16 operands, float32 addend and result, one
+// rounding), which equals fmaf on the operands converted to float32 (the
+// conversion is exact and the product of two float16 values is exact in
+// float32).
+__device__ __forceinline__ float fma_h2_f32(uint32_t a, uint32_t b, float c) {
+    float d;
+    asm("{\n\t.reg .f16 al, ah, bl, bh;\n\t"
+        "mov.b32 {al, ah}, %1;\n\t"
+        "mov.b32 {bl, bh}, %2;\n\t"
+        "fma.rn.f32.f16 %0, al, bl, %3;\n\t"
+        "fma.rn.f32.f16 %0, ah, bh, %0;\n\t}"
+        : "=f"(d) : "r"(a), "r"(b), "f"(c));
+    return d;
+}
 template <int K8>
 __global__ void __launch_bounds__(256) k_prop_score_map_s(const uint4 *ET, const uint4 *EQ, size_t pstride,
                                                           int npair, int d, const int16_t *srcmap, int nrot,
@@ -464,31 +480,19 @@ __global__ void __launch_bounds__(256) k_prop_score_map_s(const uint4 *ET, const
                 const int s = r0 + j < rend ? (int)__ldg(srcmap + (size_t)(r0 + j) * n + v) : -1;
                 sj[j] = s < 0 ? n : s;
             }
-            float2 t[K8][4];
+            uint4 t[K8];
 #pragma unroll
-            for (int g = 0; g < K8; ++g) {
-                const uint4 a = __ldg(et + (size_t)v * K8 + g);
-                t[g][0] = __half22float2(*(const __half2 *)&a.x);
-                t[g][1] = __half22float2(*(const __half2 *)&a.y);
-                t[g][2] = __half22float2(*(const __half2 *)&a.z);
-                t[g][3] = __half22float2(*(const __half2 *)&a.w);
-            }
+            for (int g = 0; g < K8; ++g) t[g] = __ldg(et + (size_t)v * K8 + g);
 #pragma unroll
             for (int j = 0; j < kScRPB; ++j) {
 #pragma unroll
                 for (int g = 0; g < K8; ++g) {
                     const uint4 b = sq[(size_t)sj[j] * K8 + g];
-                    const float2 q0 = __half22float2(*(const __half2 *)&b.x), q1 = __half22float2(*(const __half2 *)&b.y);
-                    const float2 q2 = __half22float2(*(const __half2 *)&b.z), q3 = __half22float2(*(const __half2 *)&b.w);
                     float a = acc[j];
-                    a = fmaf(t[g][0].x, q0.x, a);
-                    a = fmaf(t[g][0].y, q0.y, a);
-                    a = fmaf(t[g][1].x, q1.x, a);
-                    a = fmaf(t[g][1].y, q1.y, a);
-                    a = fmaf(t[g][2].x, q2.x, a);
-                    a = fmaf(t[g][2].y, q2.y, a);
-                    a = fmaf(t[g][3].x, q3.x, a);
-                    a = fmaf(t[g][3].y, q3.y, a);
+                    a = fma_h2_f32(t[g].x, b.x, a);
+                    a = fma_h2_f32(t[g].y, b.y, a);
+                    a = fma_h2_f32(t[g].z, b.z, a);
+                    a = fma_h2_f32(t[g].w, b.w, a);
                     acc[j] = a;
                 }
             }
