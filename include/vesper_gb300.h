@@ -279,6 +279,36 @@ int vesper_rescore_batch_dev(const double *tdata, const float *tvec, const doubl
                              void *workspace, size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Refinement on the device (the reference's refinement set and its top-N,
+ * VESPER_1_prob_new.py:689-740, with get_score's wrapped translation,
+ * :1323-1329), for callers that keep the whole alignment on the device.
+ *
+ * vesper_refine_slots: for n pairs with topn global top angles each, given as
+ * grid indices tg int64 [n][topn] (-1: none) into grid_rows int64 [ngrid]
+ * (each grid angle's row on a lattice of lattice_n steps per axis, row =
+ * (x L + y) L + z), and offsets int64 [27][3] in lattice steps: slot
+ * t = (i topn + k) 27 + o is top k's row plus offset o, valid where
+ * x < L, y < L, z < L/2 before negative coordinates wrap by +L and the top
+ * exists.  Writes crow int64 [n topn 27] (0 for an invalid slot), valid uint8
+ * [same] and rmats float [same][3][3] = lattice[crow] (lattice float
+ * [L^3][3][3]).  All pointers DEVICE.
+ *
+ * vesper_refine_pick: one pair's slots after their search (scores float and
+ * lin int32 [nslot][nscore], column 0 used): the stable top-N over the valid
+ * slots (the others read -inf; ties to the lower slot; -1 past the slots) in
+ * rtop int32 [topn], and per pick (slot 0 standing in for -1) its row int64,
+ * score float, lin int64, rotation mats float [topn][3][3] = lattice[row] and
+ * trans int32 [topn][3] = (lin / d^2, lin / d % d, lin % d), each t > d/2
+ * taken as t - d.  All pointers DEVICE.  No counterparts in the reference.
+ * ------------------------------------------------------------------------- */
+int vesper_refine_slots(const int64_t *tg, int n, int topn, const int64_t *grid_rows, int ngrid, const int64_t *offsets,
+                        int lattice_n, const float *lattice, int64_t *crow, uint8_t *valid, float *rmats,
+                        void *stream);
+int vesper_refine_pick(const float *scores, const int32_t *lin, int nscore, const uint8_t *valid, const int64_t *crow,
+                       int nslot, int topn, const float *lattice, int d, int32_t *rtop, int64_t *rows, float *rscore,
+                       int64_t *rlin, float *mats, int32_t *trans, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Probability-map hole filling (interpolate, interpolation_functions.py:6-135)
  * in place on a DEVICE float32 [nx][ny][nz][nch] array: the parity of the
  * first voxel (C order) with channel 0 > 0 fixes the sampled lattice; zero

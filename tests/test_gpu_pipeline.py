@@ -328,3 +328,67 @@ def test_graph_late_stage_many_pairs_of_one_side(dev):
             assert [m.vec_trans for m in r.models] == [m.vec_trans for m in a.models]
             assert [m.dot_score for m in r.models] == [m.dot_score for m in a.models]
             assert [m.cc for m in r.models] == [m.cc for m in a.models]
+
+
+def test_refine_slots_and_pick_match_tensor_formulation(dev):
+    """vesper_refine_slots and vesper_refine_pick against the same steps in
+    torch tensor arithmetic: slots of the 5-degree lattice (filter before the
+    wrap, dropped slots row 0), stable masked top-N with ties to the lower
+    slot, the picks' rows, scores, translations and wrapped translations."""
+    import ctypes
+    from vesper_python_gb300 import _native, align
+    from vesper_python_gb300 import vesper as vg
+    c_ = lambda t: ctypes.c_void_p(t.data_ptr())
+    rng = np.random.default_rng(11)
+    L = vg.LATTICE_N
+    al = align.Aligner(dev)
+    lat = vg.lattice_rot_matrices_device(dev)
+    grid_rows = al._grid_rows(10.0, vg.calc_angle_comb(10.0))
+    off = al._ref_offsets()
+    n, N, d, nscore = 5, 10, 30, 1
+    ngrid = int(grid_rows.shape[0])
+    tg_h = rng.integers(0, ngrid, size=(n, N))
+    tg_h[1, 7:] = -1
+    tg_h[2, 0] = 0                                  # the grid's first angle: offsets wrap and drop
+    tg_h[3, :] = ngrid - 1                          # the last: z = 175 drops z + 5
+    tg = dev.to_dev(tg_h.astype(np.int64))
+    crow = torch.empty((n, N * 27), dtype=torch.int64, device=dev.device)
+    valid = torch.empty((n, N * 27), dtype=torch.bool, device=dev.device)
+    rmats = torch.empty((n, N * 27, 3, 3), dtype=torch.float32, device=dev.device)
+    _native.check(dev.lib.vesper_refine_slots(c_(tg), n, N, c_(grid_rows), ngrid, c_(off), L, c_(lat), c_(crow),
+                                              c_(valid), c_(rmats), dev.stream))
+    # the tensor formulation
+    rows = grid_rows.index_select(0, tg.clamp(min=0).reshape(-1)).reshape(n, N)
+    base = torch.stack([rows // (L * L), (rows // L) % L, rows % L], dim=2)
+    cand = base[:, :, None, :] + off[None, None, :, :]
+    v_ref = (cand[..., 0] < L) & (cand[..., 1] < L) & (cand[..., 2] < L // 2) & (tg >= 0)[:, :, None]
+    cand = torch.where(cand < 0, cand + L, cand)
+    c_ref = (cand[..., 0] * L + cand[..., 1]) * L + cand[..., 2]
+    v_ref = v_ref.reshape(n, N * 27)
+    c_ref = torch.where(v_ref, c_ref.reshape(n, N * 27), torch.zeros_like(v_ref, dtype=torch.int64))
+    assert torch.equal(valid, v_ref) and torch.equal(crow, c_ref)
+    assert torch.equal(rmats, lat.index_select(0, c_ref.reshape(-1)).reshape(n, N * 27, 3, 3))
+    assert bool((~valid[1, 7 * 27:]).all()) and bool((~valid[3]).any())
+    # picks, with exact ties among the scores
+    RS = dev.to_dev(rng.integers(0, 40, size=(n, N * 27, nscore)).astype(np.float32))
+    RL = dev.to_dev(rng.integers(0, d ** 3, size=(n, N * 27, nscore)).astype(np.int32))
+    for i in range(n):
+        out = [torch.empty(N, dtype=torch.int32, device=dev.device), torch.empty(N, dtype=torch.int64, device=dev.device),
+               torch.empty(N, dtype=torch.float32, device=dev.device), torch.empty(N, dtype=torch.int64, device=dev.device),
+               torch.empty((N, 3, 3), dtype=torch.float32, device=dev.device),
+               torch.empty((N, 3), dtype=torch.int32, device=dev.device)]
+        _native.check(dev.lib.vesper_refine_pick(c_(RS[i]), c_(RL[i]), nscore, c_(valid[i]), c_(crow[i]), N * 27, N,
+                                                 c_(lat), d, *[c_(t) for t in out], dev.stream))
+        masked = torch.where(valid[i], RS[i, :, 0], torch.full_like(RS[i, :, 0], float("-inf")))
+        rtop = vg.topn_device(masked.contiguous(), N, dev=dev)
+        sel = rtop.to(torch.int64).clamp(min=0)
+        r_rows = crow[i].gather(0, sel)
+        r_lin = RL[i, :, 0].to(torch.int64).gather(0, sel)
+        t = torch.stack([r_lin // (d * d), (r_lin // d) % d, r_lin % d], dim=1)
+        trd = torch.where(2 * t > d, t - d, t).to(torch.int32)
+        assert torch.equal(out[0], rtop)
+        assert torch.equal(out[1], r_rows)
+        assert torch.equal(out[2], RS[i, :, 0].gather(0, sel))
+        assert torch.equal(out[3], r_lin)
+        assert torch.equal(out[4], lat.index_select(0, r_rows))
+        assert torch.equal(out[5], trd)

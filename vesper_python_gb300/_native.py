@@ -128,6 +128,8 @@ SIGNATURES = {
     "vesper_rescore_batch_workspace_size": [_i, _i, _psz],
     "vesper_rescore_batch": [_vp, _vp, _d, _d, _d, _vp, _vp, _i, _vp, _i, _vp, _vp, _sz, _vp],
     "vesper_rescore_batch_dev": [_vp, _vp, _vp, _vp, _vp, _i, _vp, _i, _vp, _vp, _sz, _vp],
+    "vesper_refine_slots": [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp],
+    "vesper_refine_pick": [_vp, _vp, _i, _vp, _vp, _i, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "vesper_prob_interpolate": [_vp, _i, _i, _i, _i, _vp, _sz, _vp],
     "vesper_prob_interpolate_found": [_vp, _vp, _vp],
     "vesper_prop_field": [_vp, _vp, _i, _i, _vp, _vp],

@@ -442,6 +442,7 @@ class Aligner:
         return allm, [int(c) for c in counts], dev.to_dev_async(local)
 
     FV_STREAMS = 4
+    LATE_MAX_BATCH = 0       # batch cap of the refinement searches that run on the side streams (0: none)
 
     def _side_streams(self):
         if getattr(self, "_side", None) is None:
@@ -615,25 +616,26 @@ class Aligner:
         grid_rows = self._grid_rows(p.A, None)
         off = self._ref_offsets()
         self._mark("refine")
+        c_ = ctypes.c_void_p
         tg = torch.stack([st.tg for st in P])                                  # [n, N] grid indices
-        rows = grid_rows.index_select(0, tg.clamp(min=0).reshape(-1)).reshape(n, N)
-        base = torch.stack([rows // (L * L), (rows // L) % L, rows % L], dim=2)  # [n, N, 3]
-        cand = base[:, :, None, :] + off[None, None, :, :]                     # [n, N, 27, 3]
-        valid = (cand[..., 0] < L) & (cand[..., 1] < L) & (cand[..., 2] < L // 2) & (tg >= 0)[:, :, None]
-        cand = torch.where(cand < 0, cand + L, cand)
-        crow = (cand[..., 0] * L + cand[..., 1]) * L + cand[..., 2]
-        valid = valid.reshape(n, N * 27)
-        crow = torch.where(valid, crow.reshape(n, N * 27), torch.zeros_like(valid, dtype=torch.int64))
-        rmats = lat.index_select(0, crow.reshape(-1)).reshape(n, N * 27, 3, 3)
+        # the refinement slots of every pair (vesper_refine_slots)
+        crow = torch.empty((n, N * 27), dtype=torch.int64, device=dev.device)
+        valid = torch.empty((n, N * 27), dtype=torch.bool, device=dev.device)
+        rmats = torch.empty((n, N * 27, 3, 3), dtype=torch.float32, device=dev.device)
+        _native.check(self.lib.vesper_refine_slots(c_(tg.data_ptr()), n, N, c_(grid_rows.data_ptr()),
+                                                   int(grid_rows.shape[0]), c_(off.data_ptr()), L,
+                                                   c_(lat.data_ptr()), c_(crow.data_ptr()), c_(valid.data_ptr()),
+                                                   c_(rmats.data_ptr()), dev.stream))
+        P[0].launches += 1
         nscore = dev.lib.vesper_search_nscore(vg.MODE_CODES[mode], 0)
         RS = torch.empty((n, N * 27, nscore), dtype=torch.float32, device=dev.device)
         RL = torch.empty((n, N * 27, nscore), dtype=torch.int32, device=dev.device)
-        # every pair's chain (search of its slots, top-N, gather and float64
-        # rescoring of the refined models) on one of FV_STREAMS side streams:
-        # the chains are short launches that fill little of the GPU, so pairs
-        # overlap; the streams fork from and join the current stream (also
-        # inside a CUDA-graph capture).  The shared inputs above are freed only
-        # after the join.
+        # every pair's chain (search of its slots, top-N and picks, gather and
+        # float64 rescoring of the refined models) on one of FV_STREAMS side
+        # streams: the chains are short launches that fill little of the GPU,
+        # so pairs overlap; the streams fork from and join the current stream
+        # (also inside a CUDA-graph capture).  The shared inputs above are
+        # freed only after the join.
         cur = torch.cuda.current_stream(dev.device)
         capturing = torch.cuda.is_current_stream_capturing()
         side = self._side_streams()
@@ -643,31 +645,31 @@ class Aligner:
             d = st.dim
             with torch.cuda.stream(side[i % len(side)]):
                 vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats[i], batch=p.batch, dev=dev,
-                                 tuned=True, out=(RS[i], RL[i]))
-                masked = torch.where(valid[i], RS[i, :, 0], torch.full_like(RS[i, :, 0], float("-inf")))
-                rtop = vg.topn_device(masked.contiguous(), N, dev=dev)
-                sel = rtop.to(torch.int64).clamp(min=0)
-                st.rtop, st.r_rows = rtop, crow[i].gather(0, sel)
-                st.r_score = RS[i, :, 0].gather(0, sel)
-                st.r_lin = RL[i, :, 0].to(torch.int64).gather(0, sel)
-                mm = lat.index_select(0, st.r_rows)
+                                 tuned=True, out=(RS[i], RL[i]), max_batch=self.LATE_MAX_BATCH)
+                st.rtop = torch.empty(N, dtype=torch.int32, device=dev.device)
+                st.r_rows = torch.empty(N, dtype=torch.int64, device=dev.device)
+                st.r_score = torch.empty(N, dtype=torch.float32, device=dev.device)
+                st.r_lin = torch.empty(N, dtype=torch.int64, device=dev.device)
+                mm = torch.empty((N, 3, 3), dtype=torch.float32, device=dev.device)
+                trd = torch.empty((N, 3), dtype=torch.int32, device=dev.device)   # wrapped as get_score (:1323-1329)
+                _native.check(self.lib.vesper_refine_pick(
+                    c_(RS[i].data_ptr()), c_(RL[i].data_ptr()), nscore, c_(valid[i].data_ptr()),
+                    c_(crow[i].data_ptr()), N * 27, N, c_(lat.data_ptr()), d, c_(st.rtop.data_ptr()),
+                    c_(st.r_rows.data_ptr()), c_(st.r_score.data_ptr()), c_(st.r_lin.data_ptr()), c_(mm.data_ptr()),
+                    c_(trd.data_ptr()), dev.stream))
                 gd, gv, _ = vg.rot_gather_device(st.qdata, st.qvec, mm, dev=dev)
-                lin = st.r_lin
-                t = torch.stack([lin // (d * d), (lin // d) % d, lin % d], dim=1)
-                trd = torch.where(2 * t > d, t - d, t).to(torch.int32).contiguous()   # wrapped as get_score (:1323-1329)
                 st.res = torch.empty((N, 8), dtype=torch.float64, device=dev.device)
                 ws = dev.workspace(("rescore_batch", i, d, N),
                                    _native.size_query("vesper_rescore_batch_workspace_size", d, N))
                 _native.check(self.lib.vesper_rescore_batch_dev(
-                    ctypes.c_void_p(st.tdata.data_ptr()), ctypes.c_void_p(st.tvec.data_ptr()),
-                    ctypes.c_void_p(stats[i].data_ptr()), ctypes.c_void_p(gd.data_ptr()),
-                    ctypes.c_void_p(gv.data_ptr()), d, ctypes.c_void_p(trd.data_ptr()), N,
-                    ctypes.c_void_p(st.res.data_ptr()), ctypes.c_void_p(ws.data_ptr()), ws.numel(), dev.stream))
+                    c_(st.tdata.data_ptr()), c_(st.tvec.data_ptr()), c_(stats[i].data_ptr()), c_(gd.data_ptr()),
+                    c_(gv.data_ptr()), d, c_(trd.data_ptr()), N, c_(st.res.data_ptr()), c_(ws.data_ptr()),
+                    ws.numel(), dev.stream))
                 if self.pair_events is not None and not capturing:
                     e = torch.cuda.Event(enable_timing=True)
                     e.record()
                     self.pair_events.append(e)
-            st.launches += self._search_launches(d, mode, N * 27, p.batch) + 7
+            st.launches += self._search_launches(d, mode, N * 27, p.batch, self.LATE_MAX_BATCH) + 7
             if not capturing:
                 for tt in (st.rtop, st.r_rows, st.r_score, st.r_lin, st.res):
                     tt.record_stream(cur)    # made on a side stream, read on this one
@@ -875,12 +877,14 @@ class Aligner:
         elif p.proposal is not None:
             st.z = torch.zeros((), dtype=torch.float32, device=self.dev.device)
 
-    def _search_launches(self, dim, mode, nrot, batch):
+    def _search_launches(self, dim, mode, nrot, batch, max_batch=0):
         if batch <= 0:
             from . import autotune
             t = autotune.cached(dim, mode, self.dev)
             if t and t.get("batch"):
                 batch = int(t["batch"])
+                if max_batch > 0:
+                    batch = min(batch, int(max_batch))
         return vg.search_plan(dim, mode, batch, nrot, None, self.dev)[1]
 
     def align_host_many(self, items, p: AlignParams, graph: bool = False):
