@@ -441,8 +441,10 @@ class Aligner:
         allm = vg.lattice_rot_matrices_device(dev).index_select(0, dev.to_dev_async(rows))
         return allm, [int(c) for c in counts], dev.to_dev_async(local)
 
-    FV_STREAMS = 4
+    FV_STREAMS = 8
     LATE_MAX_BATCH = 0       # batch cap of the refinement searches that run on the side streams (0: none)
+    GLOBAL_SIDE = False      # the proposal form's global searches on the side streams too
+    GLOBAL_MAX_BATCH = 0     # and their batch cap (0: none)
 
     def _side_streams(self):
         if getattr(self, "_side", None) is None:
@@ -511,8 +513,25 @@ class Aligner:
             nscore = dev.lib.vesper_search_nscore(vg.MODE_CODES[mode], 0)
             S = torch.empty((n, k, nscore), dtype=torch.float32, device=dev.device)
             L = torch.empty((n, k, nscore), dtype=torch.int32, device=dev.device)
-            for i, st in enumerate(P):
-                self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
+            if self.GLOBAL_SIDE and self.group is None and self.profile is None:
+                # the pairs' searches on the side streams (batch capped so that
+                # the concurrent searches' scratch stays near the L2 size)
+                cur = torch.cuda.current_stream(dev.device)
+                capturing = torch.cuda.is_current_stream_capturing()
+                side = self._side_streams()
+                for sd in side:
+                    sd.wait_stream(cur)
+                for i, st in enumerate(P):
+                    with torch.cuda.stream(side[i % len(side)]):
+                        self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False,
+                                            max_batch=self.GLOBAL_MAX_BATCH)
+                    if not capturing:
+                        st.top.record_stream(cur)
+                for sd in side:
+                    cur.wait_stream(sd)
+            else:
+                for i, st in enumerate(P):
+                    self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
             sc0 = S[:, :, 0]
             z = (sc0.max(dim=1).values - sc0.mean(dim=1)) / (sc0.std(dim=1) + 1e-30)
             for i, st in enumerate(P):
@@ -851,7 +870,7 @@ class Aligner:
                 # 2 fields + (4 layers + vmajor + top-k) shared by the group + scoring
                 st.launches += 3 + (6 if i == 0 else 0)
 
-    def _global_search(self, p, st, mats, nang, out=None, zscore=True):
+    def _global_search(self, p, st, mats, nang, out=None, zscore=True, max_batch=0):
         """Search of the given rotations, top-N and (subset searches, unless
         the caller batches it) the z-score of the best exact score over the
         subset; all on the device."""
@@ -865,8 +884,9 @@ class Aligner:
             st.scores, st.lin = sc, ln
         else:
             st.scores, st.lin = vg.search_device(st.spec, st.qdata, st.qvec, p.mode, st.ave, mats, batch=p.batch,
-                                                 dev=self.dev, profile=self.profile, tuned=True, out=out)
-        st.launches += self._search_launches(st.dim, p.mode, int(mats.shape[0]), p.batch)
+                                                 dev=self.dev, profile=self.profile, tuned=True, out=out,
+                                                 max_batch=max_batch)
+        st.launches += self._search_launches(st.dim, p.mode, int(mats.shape[0]), p.batch, max_batch)
         st.top = vg.topn_device(st.scores, p.N, dev=self.dev)
         st.launches += 1
         if not zscore:
