@@ -443,7 +443,7 @@ class Aligner:
 
     FV_STREAMS = 8
     LATE_MAX_BATCH = 0       # batch cap of the refinement searches that run on the side streams (0: none)
-    GLOBAL_SIDE = False      # the proposal form's global searches on the side streams too
+    GLOBAL_SIDE = True       # the proposal form's global searches on the side streams too
     GLOBAL_MAX_BATCH = 0     # and their batch cap (0: none)
 
     def _side_streams(self):
