@@ -745,7 +745,6 @@ class Aligner:
         PCC never come here, so every score scale is 1."""
         mode = p.mode
         assert mode not in ("CC", "PCC")
-        L = vg.LATTICE_N
         self._mark("results")
         late = self._fetch_start([[st.rtop, st.r_rows, st.r_score, st.r_lin, st.res] for st in P], slot=1)
         glob = self._fetch_finish(gh)
@@ -774,15 +773,13 @@ class Aligner:
             for k, rk in enumerate(rtop.tolist()):
                 if rk < 0:
                     continue
-                row = rows_l[k]
-                ang = (np.float64(float(row // (L * L)) * vg.LATTICE_STEP),
-                       np.float64(float((row // L) % L) * vg.LATTICE_STEP),
-                       np.float64(float(row % L) * vg.LATTICE_STEP))
+                ang = self._lattice_angle(rows_l[k])
                 sc = float(score_l[k] * scale * rd3)
                 tr = vg.unravel(lin_l[k], st.dim)
                 rr = res_l[k]
-                models.append(Model(ang, sc, tr, float(np.float64(rr[0]) / rr[1]), rr[2], rr[3], rr[4],
-                                    (st.c1, st.c2, p.s, st.dim)))
+                # Nm / total (numpy's division where total is 0: inf or nan with its warning)
+                ov = rr[0] / rr[1] if rr[1] != 0.0 else float(np.float64(rr[0]) / rr[1])
+                models.append(Model(ang, sc, tr, ov, rr[2], rr[3], rr[4], (st.c1, st.c2, p.s, st.dim)))
             self.launches += st.launches
             ave_s, std_s, top_list = head[i]
             out.append(AlignResult(st.dim, std_s, ave_s, top_list, models, st.launches))
@@ -791,6 +788,18 @@ class Aligner:
         self._mark("end")
         self._close_marks()
         return out
+
+    def _lattice_angle(self, row):
+        """The (x, y, z) angle tuple (np.float64 degrees) of a 5-degree lattice
+        row, cached per row."""
+        cache = self.__dict__.setdefault("_lattice_angle_cache", {})
+        a = cache.get(row)
+        if a is None:
+            L = vg.LATTICE_N
+            a = cache[row] = (np.float64(float(row // (L * L)) * vg.LATTICE_STEP),
+                              np.float64(float((row // L) % L) * vg.LATTICE_STEP),
+                              np.float64(float(row % L) * vg.LATTICE_STEP))
+        return a
 
     def _angle_tuples(self, A, angle_comb):
         """The rows of the angle grid of step A as tuples (cached per step)."""
