@@ -75,10 +75,11 @@ SUB_STEPS, SUB_WARMUP = 5, 3    # timed / warm-up steps of each sub-configuratio
 MODE_NAMES = {"V": "VecProduct", "O": "Overlap", "C": "CC", "P": "PCC", "L": "Laplacian"}
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per rotation of the
-# dominant search kernel (pass A of the register two-step passes), mode V, by
-# grid side, from ncu captures of ``bench.py --case search<d>`` (one launch of
-# k_rpass_a at the search's own batch; profiles/k_rpass_a_side<d>_*.md).
-PASS_A_DRAM_PER_ROT = {28: 48521, 30: 3778, 32: 8116, 75: 4281444}
+# dominant search kernel (search pass A), mode V, by grid side, from ncu
+# captures of ``bench.py --case search<d> <nrot> <batch>`` at the batches the
+# workloads run (256 rotations per launch at sides 28-32, 128 at 75), caches
+# left as the previous launches leave them (profiles/search_pass_a_dram.md).
+PASS_A_DRAM_PER_ROT = {28: 264845, 30: 266378, 32: 290951, 75: 4726406}
 
 
 def parse():
