@@ -102,6 +102,9 @@ def parse():
                     help="headline value with eager launches instead of the CUDA graphs")
     ap.add_argument("--no-graph-replay", action="store_true",
                     help="skip the second form's measurement (eager, or graphs with --eager; profiler lists)")
+    ap.add_argument("--sub-config", action="store_true",
+                    help="run --workload as a sub-configuration of the default line (its steps capped at "
+                         f"{SUB_STEPS} after {SUB_WARMUP} warm-up) and print its object")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one more step of the headline form between cudaProfilerStart and cudaProfilerStop "
                          "(for ncu --profile-from-start off: a launch list of exactly one step)")
@@ -542,12 +545,29 @@ def run_gb300(args):
         torch.cuda.empty_cache()
         line["configs"] = {
             "pair200_s2_a10": config_pair200(args, dev),
-            "uneven64_s4_a15": run_uneven(args, sub=True),
-            "prob128_s3_a15": run_prob(args, sub=True),
+            "uneven64_s4_a15": run_sub_process(args, "uneven64_s4_a15"),
+            "prob128_s3_a15": run_sub_process(args, "prob128_s3_a15"),
         }
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_sub_process(args, workload):
+    """One sub-configuration in a fresh process (``--sub-config``): its
+    timings do not inherit this process's allocations, graphs and threads.
+    Returns its JSON object (or the error)."""
+    import subprocess
+    cmd = [sys.executable, os.path.abspath(__file__), "--workload", workload, "--steps", str(args.steps),
+           "--warmup", str(args.warmup), "--sub-config"]
+    if args.no_cpu_baseline:
+        cmd.append("--no-cpu-baseline")
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE")}
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"error": f"exit {r.returncode}: " + (r.stderr.strip().splitlines() or ["no output"])[-1][:300]}
+    return json.loads(lines[-1])
 
 
 # ---------------------------------------------------------------------------
@@ -1153,8 +1173,12 @@ if __name__ == "__main__":
     elif a.impl == "reference":
         run_reference(a)
     elif a.workload == "uneven64_s4_a15":
-        run_uneven(a)
+        sub_line = run_uneven(a, sub=a.sub_config)
+        if a.sub_config:
+            print(json.dumps(sub_line), flush=True)
     elif a.workload == "prob128_s3_a15":
-        run_prob(a)
+        sub_line = run_prob(a, sub=a.sub_config)
+        if a.sub_config:
+            print(json.dumps(sub_line), flush=True)
     else:
         run_gb300(a)
