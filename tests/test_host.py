@@ -278,3 +278,34 @@ def test_show_vec_writes_the_reference_files(golden_dir, tmp_path):
         files = sorted(x.name for x in out.iterdir())
         assert files == [str(g[f"c{k}_name"])]
         assert (out / files[0]).read_text() == str(g[f"c{k}_text"])
+
+
+def test_size_grids_matches_size_grid():
+    """The aligner's batched grid sizing gives every map what the per-map
+    mrc_set_vox_size step gives (the same float64 operations): sides, new
+    origins and centres bit for bit, the float32 origins, and the empty-map
+    error."""
+    from vesper_python_gb300 import align
+    rng = np.random.default_rng(5)
+    for _ in range(50):
+        n = int(rng.integers(1, 20))
+        r2 = rng.uniform(10, 5000, size=(n, 2))
+        prh = np.zeros((n, 4), np.uint64)
+        prh[:, 0], prh[:, 2] = r2.view(np.uint64)[:, 0], r2.view(np.uint64)[:, 1]
+        prh[:, 1], prh[:, 3] = 5, 7
+        cents = [tuple(np.array([x * 0.5 for x in rng.integers(20, 300, 3)]) for _ in range(2)) for _ in range(n)]
+        widths = [tuple(float(np.float32(rng.uniform(0.5, 3))) for _ in range(2)) for _ in range(n)]
+        origs = [tuple(tuple(rng.uniform(-50, 50, 3)) for _ in range(2)) for _ in range(n)]
+        s = float(rng.choice([2.0, 3.0, 4.0, 7.0]))
+        dims, norig, ncent, o32 = align._size_grids(prh, cents, widths, origs, s)
+        for i in range(n):
+            for m in range(2):
+                o = np.array([np.float32(v) for v in origs[i][m]])
+                d, no, c = align._size_grid(prh[i, 2 * m], prh[i, 2 * m + 1], cents[i][m], widths[i][m], o, s)
+                assert d == dims[i][m]
+                assert np.array_equal(no, norig[i, m]) and no.dtype == norig.dtype
+                assert np.array_equal(c, ncent[i, m]) and c.dtype == ncent.dtype
+                assert np.array_equal(o, o32[i, m]) and o.dtype == o32.dtype
+    prh[0, 3] = 0
+    with pytest.raises(ValueError, match="empty sequence"):
+        align._size_grids(prh, cents, widths, origs, s)

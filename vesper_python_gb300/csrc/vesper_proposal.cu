@@ -47,20 +47,23 @@ __global__ void k_conv_fwd(const float *in, int cin, const __nv_bfloat16 *W, con
     out[(size_t)co * n + v] = relu ? fmaxf(acc, 0.f) : acc;
 }
 
-// The same layer with COG output channels per thread: one input load feeds
-// COG products, the block's COG x cin x 27 weights sit in shared memory as
-// float32 in [cin][27][COG] order (every thread reads the same COG weights at
-// the same step: one 16-byte broadcast load per four), and the 27 neighbour
-// offsets and their in-grid mask are computed once per voxel.  The summation
-// order per output is that of k_conv_fwd (bias, then ci, then tap), so the
+// The same layer with COG = 4 output channels and ZS consecutive z voxels per
+// thread: the block's COG x cin x 27 weights sit in shared memory as float32 in
+// [cin][27][channel] order (each tap's four weights are one 16-byte broadcast
+// load), and for each input channel and (x, y) neighbour row the ZS + 2 input
+// values of the row are loaded once, so each load feeds up to 3 x COG products
+// and each weight load ZS x COG.  Taps outside the grid are skipped per voxel
+// as in k_conv_fwd, in the same order (bias, then ci, then tap), so the
 // results are the same bits.
-template <int COG>
-__global__ void __launch_bounds__(128) k_conv_fwd_g(const float *in, int cin, const __nv_bfloat16 *W,
+constexpr int kConvCOG = 4;
+constexpr int kConvZS = 4;   // measured over the prop128 step: 4 beat 2 and 1 (one voxel per thread)
+template <int COG, int ZS>
+__global__ void __launch_bounds__(128) k_conv_fwd_s(const float *in, int cin, const __nv_bfloat16 *W,
                                                     const float *bias, int cout, int d, int relu, float *out) {
-    static_assert(COG % 4 == 0, "COG: a multiple of 4");
-    extern __shared__ float4 wsh4[];   // [cin][27][COG / 4]
+    static_assert(COG == 4, "k_conv_fwd_s: 4 output channels per thread");
+    extern __shared__ float4 wsh4[];   // [cin][27]
     float *wsh = (float *)wsh4;
-    const int n = d * d * d;
+    const int n = d * d * d, nzs = (d + ZS - 1) / ZS;
     const int co0 = blockIdx.y * COG;
     in += (size_t)blockIdx.z * cin * n;
     out += (size_t)blockIdx.z * cout * n;
@@ -69,37 +72,57 @@ __global__ void __launch_bounds__(128) k_conv_fwd_g(const float *in, int cin, co
         wsh[t * COG + j] = __bfloat162float(W[(size_t)co0 * cin * 27 + i]);
     }
     __syncthreads();
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
-    const int x = v / (d * d), y = (v / d) % d, z = v % d;
-    uint32_t mask = 0u;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= d * d * nzs) return;
+    const int x = u / (d * nzs), y = (u / nzs) % d, z0 = (u % nzs) * ZS;
+    float acc[ZS][COG];
 #pragma unroll
-    for (int o = 0; o < 27; ++o) {
-        const int xx = x + o / 9 - 1, yy = y + (o / 3) % 3 - 1, zz = z + o % 3 - 1;
-        if (xx >= 0 && yy >= 0 && zz >= 0 && xx < d && yy < d && zz < d) mask |= 1u << o;
-    }
-    float acc[COG];
+    for (int i = 0; i < ZS; ++i)
 #pragma unroll
-    for (int j = 0; j < COG; ++j) acc[j] = bias ? bias[co0 + j] : 0.f;
+        for (int j = 0; j < COG; ++j) acc[i][j] = bias ? bias[co0 + j] : 0.f;
     for (int ci = 0; ci < cin; ++ci) {
-        const float *src = in + (size_t)ci * n + v;
-        const float4 *w = wsh4 + (size_t)ci * 27 * (COG / 4);
+        const float *src = in + (size_t)ci * n;
+        const float4 *w = wsh4 + (size_t)ci * 27;
 #pragma unroll
-        for (int o = 0; o < 27; ++o) {
-            if (!(mask & (1u << o))) continue;
-            const float val = src[((o / 9 - 1) * d + ((o / 3) % 3 - 1)) * d + (o % 3 - 1)];
+        for (int ox = 0; ox < 3; ++ox) {
+            const int xx = x + ox - 1;
+            if (xx < 0 || xx >= d) continue;
 #pragma unroll
-            for (int q = 0; q < COG / 4; ++q) {
-                const float4 w4 = w[o * (COG / 4) + q];
-                acc[4 * q + 0] = fmaf(w4.x, val, acc[4 * q + 0]);
-                acc[4 * q + 1] = fmaf(w4.y, val, acc[4 * q + 1]);
-                acc[4 * q + 2] = fmaf(w4.z, val, acc[4 * q + 2]);
-                acc[4 * q + 3] = fmaf(w4.w, val, acc[4 * q + 3]);
+            for (int oy = 0; oy < 3; ++oy) {
+                const int yy = y + oy - 1;
+                if (yy < 0 || yy >= d) continue;
+                const float *row = src + ((size_t)xx * d + yy) * d;
+                float val[ZS + 2];
+#pragma unroll
+                for (int e = 0; e < ZS + 2; ++e) {
+                    const int zz = z0 + e - 1;
+                    val[e] = zz >= 0 && zz < d ? row[zz] : 0.f;
+                }
+#pragma unroll
+                for (int oz = 0; oz < 3; ++oz) {
+                    const float4 w4 = w[ox * 9 + oy * 3 + oz];
+#pragma unroll
+                    for (int i = 0; i < ZS; ++i) {
+                        const int zz = z0 + i + oz - 1;
+                        if (zz < 0 || zz >= d) continue;
+                        const float v = val[i + oz];
+                        acc[i][0] = fmaf(w4.x, v, acc[i][0]);
+                        acc[i][1] = fmaf(w4.y, v, acc[i][1]);
+                        acc[i][2] = fmaf(w4.z, v, acc[i][2]);
+                        acc[i][3] = fmaf(w4.w, v, acc[i][3]);
+                    }
+                }
             }
         }
     }
 #pragma unroll
-    for (int j = 0; j < COG; ++j) out[(size_t)(co0 + j) * n + v] = relu ? fmaxf(acc[j], 0.f) : acc[j];
+    for (int i = 0; i < ZS; ++i) {
+        const int z = z0 + i;
+        if (z >= d) break;
+        const size_t v = ((size_t)x * d + y) * d + z;
+#pragma unroll
+        for (int j = 0; j < COG; ++j) out[(size_t)(co0 + j) * n + v] = relu ? fmaxf(acc[i][j], 0.f) : acc[i][j];
+    }
 }
 
 // din[ci][v] = sum_co sum_o W[co][ci][o] * g[co][v - o],  g = dout (masked by
@@ -761,14 +784,15 @@ extern "C" int vesper_prop_conv_fwd(const float *in, int cin, const void *W, con
     if (!in || !W || !out || cin < 1 || cout < 1 || d < 1 || nmap < 1 || nmap > 65535)
         return fail(VESPER_ERR_INVALID, "conv_fwd: bad args");
     const int n = d * d * d;
-    // 4 output channels per thread (measured: 8 per thread was 10 % slower over the encoder)
-    constexpr int COG = 4;
+    // 4 output channels per thread (8 measured 10 % slower over the encoder), 4 z voxels
+    constexpr int COG = kConvCOG, ZS = kConvZS;
     const size_t sm = (size_t)COG * cin * 27 * sizeof(float);
     if (cout % COG == 0 && sm <= (size_t)smem_limit()) {
-        allow_smem(k_conv_fwd_g<COG>, sm);
-        k_conv_fwd_g<COG><<<dim3((n + 127) / 128, cout / COG, nmap), 128, sm, (cudaStream_t)stream>>>(
+        const int nu = d * d * ((d + ZS - 1) / ZS);
+        allow_smem(k_conv_fwd_s<COG, ZS>, sm);
+        k_conv_fwd_s<COG, ZS><<<dim3((nu + 127) / 128, cout / COG, nmap), 128, sm, (cudaStream_t)stream>>>(
             in, cin, (const __nv_bfloat16 *)W, bias, cout, d, relu, out);
-        VG_CHECK_LAUNCH("k_conv_fwd_g");
+        VG_CHECK_LAUNCH("k_conv_fwd_s");
         return VESPER_OK;
     }
     k_conv_fwd<<<dim3((n + 127) / 128, cout, nmap), 128, 0, (cudaStream_t)stream>>>(
