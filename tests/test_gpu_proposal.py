@@ -370,3 +370,42 @@ def test_conv_forward_kernels_bit_identical(dev, relu):
     np.testing.assert_array_equal(outs[24][:, :6], outs[6])
     np.testing.assert_array_equal(outs[24][:, :3], outs[3])
     assert np.isfinite(outs[24]).all()
+
+
+@pytest.mark.parametrize("fallback_z", [None, 1e9, "mixed"])
+def test_aligner_proposal_graph_equals_eager(dev, fallback_z):
+    """The learned-proposal aligner in the graph form (the refinement graph
+    launched before the flatness test is read; pairs that fall back are
+    searched exhaustively and refined again) gives the eager form's results:
+    no fallback, every pair falling back, and a threshold between the pairs'
+    z-scores so that only some fall back."""
+    P = _prop()
+    from vesper_python_gb300 import align
+    net = P.load_weights(dev)[0]
+    items = []
+    for seed in range(30_000_100, 30_000_104):
+        m1, m2, o1, o2 = P.blob_pair_torch(seed, side=128, nblob=400, radius=40.0, device=dev.device)
+        items.append((m1, m2, 1.0, 1.0, o1, o2))
+    al = align.Aligner(dev)
+    p = align.AlignParams(t=0.1, T=0.1, g=16.0, s=3.0, A=10.0, N=10, proposal=net, proposal_fallback_z=None)
+    if fallback_z == "mixed":
+        al.align_many(items, p)
+        z = sorted(al.proposal_info["z"])
+        p.proposal_fallback_z = 0.5 * (z[1] + z[2])
+    else:
+        p.proposal_fallback_z = fallback_z
+    eager = al.align_many(items, p)
+    fb = list(al.proposal_info["fallback"])
+    if fallback_z == "mixed":
+        assert 0 < sum(fb) < len(fb)
+    elif fallback_z is not None:
+        assert all(fb)
+    for _ in range(2):
+        g = al.align_many(items, p, graph=True)
+        assert al.proposal_info["fallback"] == fb
+        for a, r in zip(eager, g):
+            assert r.top == a.top
+            assert (r.ave, r.std) == (a.ave, a.std)
+            assert [m.angle for m in r.models] == [m.angle for m in a.models]
+            assert [m.vec_trans for m in r.models] == [m.vec_trans for m in a.models]
+            assert [m.dot_score for m in r.models] == [m.dot_score for m in a.models]

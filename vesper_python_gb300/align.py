@@ -134,6 +134,25 @@ def _size_grid(dmax2_bits, count, cent, width, orig, s):
     return new_dim, new_orig, new_cent
 
 
+def _size_grids(prh, cents, widths, origs, s):
+    """_size_grid of both maps of every pair at once: prh uint64 [n][4] (radius
+    bits and count of map 1, then map 2), cents / widths / origs per pair and
+    map.  The same float64 operations element by element; returns the sides
+    (int [n][2]), new origins and centres (float64 [n][2][3]) and the origins
+    as float32 [n][2][3]."""
+    n = len(cents)
+    q = np.asarray(prh, np.uint64).reshape(n, 2, 2)
+    if (q[:, :, 1] == 0).any():
+        raise ValueError("max() arg is an empty sequence")
+    dmax = np.sqrt(np.ascontiguousarray(q[:, :, 0]).view(np.float64))
+    dmax = dmax * np.array(widths, np.float64)
+    o32 = np.array([[[np.float32(v) for v in o] for o in pair] for pair in origs], np.float32)
+    cent = np.array(cents, np.float64) * np.array(widths, np.float64)[:, :, None] + o32
+    dims = np.array([[vg.next_fast_len(int(v)) for v in row] for row in 2 * dmax / s], np.int64)
+    norig = cent - 0.5 * dims[:, :, None] * s
+    return [[int(v) for v in row] for row in dims], norig, cent, o32
+
+
 class _Pair:
     """Per-pair state of align_many between its stages."""
 
@@ -236,11 +255,13 @@ class Aligner:
         prh = prep.cpu().numpy().view(np.uint64)
         self.d2h_bytes += prep.numel() * 8
         # ---- 2. fastVEC, target statistics and spectra -------------------------
+        dims, norig, ncent, origs = _size_grids(prh, [(st.cent1, st.cent2) for st in P],
+                                                 [(st.width1, st.width2) for st in P],
+                                                 [(st.orig1, st.orig2) for st in P], p.s)
         for i, st in enumerate(P):
-            st.o1 = np.array([np.float32(v) for v in st.orig1])
-            st.o2 = np.array([np.float32(v) for v in st.orig2])
-            d1, st.no1, st.c1 = _size_grid(prh[i, 0], prh[i, 1], st.cent1, st.width1, st.o1, p.s)
-            d2, st.no2, st.c2 = _size_grid(prh[i, 2], prh[i, 3], st.cent2, st.width2, st.o2, p.s)
+            st.o1, st.o2 = origs[i, 0], origs[i, 1]
+            st.no1, st.no2, st.c1, st.c2 = norig[i, 0], norig[i, 1], ncent[i, 0], ncent[i, 1]
+            d1, d2 = dims[i]
             if d1 > d2:
                 st.dim = d1
                 st.no2 = st.c2 - 0.5 * p.s * st.dim
@@ -263,30 +284,51 @@ class Aligner:
             stats, sh = self._global_stage_graph(P, p, mats, nang), None
         else:
             stats, sh = self._global_stage(P, p, mats, nang)
+        device_late = graph and mode not in ("PCC", "CC") and p.A > 5.0 and self.group is None and \
+            self._grid_rows(p.A, angle_comb) is not None
+
+        def global_results():
+            # the global results go to the host while the refinement runs
+            return self._fetch_start([[st.scores[:, 0].contiguous(), st.lin[:, 0].contiguous(), st.top] +
+                                      ([st.order] if st.order is not None else []) for st in P], slot=0)
+
+        gh = None
         zs = None
         if p.proposal is not None:
-            zs = torch.stack([st.z for st in P]).cpu().numpy()
-            self.d2h_bytes += zs.nbytes
+            zdev = torch.stack([st.z for st in P])
+            if device_late:
+                # the refinement graph is launched before the flatness test is
+                # read back, so the device does not wait for the host; a pair
+                # that falls back to the exhaustive search (rare) is refined
+                # again below
+                zh = self._fetch_start([[zdev]], slot=2)
+                gh = global_results()
+                self._late_stage_graph(P, p, stats, mats)
+                zs = self._fetch_finish(zh)[0][0]
+            else:
+                zs = zdev.cpu().numpy()
+                self.d2h_bytes += zs.nbytes
             redo = [st for st, z in zip(P, zs) if p.proposal_fallback_z is not None and z < p.proposal_fallback_z]
             for st in redo:       # the fallback: the whole grid
                 st.order = None
                 st.fallback = True
                 self._global_search(p, st, mats, nang)
                 st.tg.copy_(st.top.to(st.tg.dtype))     # top grid indices, read by the device late stage
+            if redo and device_late:
+                gh = global_results()
+                self._late_stage_graph(P, p, stats, mats)
             self.proposal_info = {"subset": int(np.ceil(p.proposal_frac * nang)), "z": [float(z) for z in zs],
                                   "fallback": [bool(st.fallback) for st in P]}
         else:
             self.proposal_info = None
-        if graph and mode not in ("PCC", "CC") and p.A > 5.0 and self.group is None and \
-                self._grid_rows(p.A, angle_comb) is not None:
+        if device_late:
             # refinement and rescoring on the device from the top indices, no
             # host value in between, replayed as one CUDA graph.  (Eager calls
             # keep the host-driven refinement below, which searches each
             # distinct angle once: fewer rotations, one more host round trip.)
-            # the global results go to the host while the refinement runs
-            gh = self._fetch_start([[st.scores[:, 0].contiguous(), st.lin[:, 0].contiguous(), st.top] +
-                                    ([st.order] if st.order is not None else []) for st in P], slot=0)
-            self._late_stage_graph(P, p, stats, mats)
+            if gh is None:
+                gh = global_results()
+                self._late_stage_graph(P, p, stats, mats)
             return self._finish_device_late(P, p, gh, angle_comb)
         if sh is None:
             sh = stats.cpu().numpy()
