@@ -636,8 +636,9 @@ class Aligner:
         """What a captured stage depends on: input addresses and shapes, grid
         geometry, parameters, the angle grid."""
         return (tuple((st.src1.data_ptr(), st.src2.data_ptr(), tuple(st.src1.shape), tuple(st.src2.shape), st.dim,
-                       tuple(np.asarray(st.no1, np.float64)), tuple(np.asarray(st.no2, np.float64)),
-                       float(st.width1), float(st.width2), tuple(st.o1), tuple(st.o2)) for st in P),
+                       *np.asarray(st.no1, np.float64).tolist(), *np.asarray(st.no2, np.float64).tolist(),
+                       float(st.width1), float(st.width2), *np.asarray(st.o1).tolist(), *np.asarray(st.o2).tolist())
+                      for st in P),
                 (p.t, p.T, p.g, p.s, p.A, p.N, p.mode, p.batch, id(p.proposal), p.proposal_frac, p.proposal_pool),
                 mats.data_ptr())
 
