@@ -146,11 +146,18 @@ def _size_grids(prh, cents, widths, origs, s):
         raise ValueError("max() arg is an empty sequence")
     dmax = np.sqrt(np.ascontiguousarray(q[:, :, 0]).view(np.float64))
     dmax = dmax * np.array(widths, np.float64)
-    o32 = np.array([[[np.float32(v) for v in o] for o in pair] for pair in origs], np.float32)
+    o32 = np.asarray(origs, np.float64).astype(np.float32)   # each value rounded to float32 (np.float32(v))
     cent = np.array(cents, np.float64) * np.array(widths, np.float64)[:, :, None] + o32
-    dims = np.array([[vg.next_fast_len(int(v)) for v in row] for row in 2 * dmax / s], np.int64)
+    raw = (2 * dmax / s).astype(np.int64)          # int() of each (positive) value
+    dl = [[_fast_len(v) for v in row] for row in raw.tolist()]
+    dims = np.array(dl, np.int64)
     norig = cent - 0.5 * dims[:, :, None] * s
-    return [[int(v) for v in row] for row in dims], norig, cent, o32
+    return dl, norig, cent, o32
+
+
+@functools.lru_cache(maxsize=None)
+def _fast_len(n):
+    return vg.next_fast_len(n)
 
 
 class _Pair:

@@ -9,35 +9,51 @@ namespace vg {
 
 // data[data < th] = 0 (float32 compare), and the largest squared distance
 // ((i-cx)^2 + (j-cy)^2) + (k-cz)^2 of a non-zero voxel, as the bits of a
-// non-negative double (ordered like unsigned integers) via atomicMax.
-__global__ void k_prepare(float *data, int sx, int sy, int sz, float th, double cx, double cy, double cz,
-                          unsigned long long *out) {
-    const size_t n = (size_t)sx * sy * sz;
+// non-negative double (ordered like unsigned integers) via atomicMax, with
+// the count of non-zero voxels.  One warp per source row (i, j) at a time, its
+// lanes over k: the row's index arithmetic and (i-cx)^2 + (j-cy)^2 are done
+// once per row (the same float64 operations in the same order per voxel).
+// Warp w of nw strides over the rows.
+__device__ __forceinline__ void prepare_rows(float *data, int sx, int sy, int sz, float th, double cx, double cy,
+                                             double cz, unsigned long long *out, int w, int nw) {
+    const int lane = threadIdx.x & 31;
     double best = -1.0;
     unsigned long long cnt = 0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        float v = data[i];
-        if (v < th) {
-            v = 0.f;
-            data[i] = 0.f;
-        }
-        if (v != 0.f) {
-            const int k = (int)(i % sz), j = (int)((i / sz) % sy), x = (int)(i / ((size_t)sy * sz));
-            const double a = (double)x - cx, b = (double)j - cy, c = (double)k - cz;
-            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
-            best = d2 > best ? d2 : best;
-            ++cnt;
+    const int nrows = sx * sy;
+    for (int row = w; row < nrows; row += nw) {
+        const int x = row / sy, j = row - x * sy;
+        const double a = (double)x - cx, b = (double)j - cy;
+        const double ab = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
+        float *rp = data + (size_t)row * sz;
+        for (int k = lane; k < sz; k += 32) {
+            float v = rp[k];
+            if (v < th) {
+                v = 0.f;
+                rp[k] = 0.f;
+            }
+            if (v != 0.f) {
+                const double c = (double)k - cz;
+                const double d2 = __dadd_rn(ab, __dmul_rn(c, c));
+                best = d2 > best ? d2 : best;
+                ++cnt;
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
-        const double w = __shfl_down_sync(0xffffffffu, best, o);
-        best = w > best ? w : best;
+        const double v = __shfl_down_sync(0xffffffffu, best, o);
+        best = v > best ? v : best;
         cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     }
-    if ((threadIdx.x & 31) == 0 && cnt > 0) {
+    if (lane == 0 && cnt > 0) {
         atomicMax(&out[0], (unsigned long long)__double_as_longlong(best));
         atomicAdd(&out[1], cnt);
     }
+}
+
+__global__ void k_prepare(float *data, int sx, int sy, int sz, float th, double cx, double cy, double cz,
+                          unsigned long long *out) {
+    prepare_rows(data, sx, sy, sz, th, cx, cy, cz, out, (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5),
+                 (int)((gridDim.x * blockDim.x) >> 5));
 }
 
 // The same for up to kPrepMax maps in one launch: map i takes blocks
@@ -60,34 +76,9 @@ __global__ void k_prepare_many(const __grid_constant__ PrepBatch b) {
     int i = 0;
     while (i + 1 < b.nmap && b.m[i + 1].first <= (int)blockIdx.x) ++i;
     const PrepMap &m = b.m[i];
-    const int sy = m.s[1], sz = m.s[2];
-    const size_t n = (size_t)m.s[0] * sy * sz;
-    const size_t nthr = (size_t)(b.m[i + 1].first - m.first) * blockDim.x;
-    double best = -1.0;
-    unsigned long long cnt = 0;
-    for (size_t e = (size_t)(blockIdx.x - m.first) * blockDim.x + threadIdx.x; e < n; e += nthr) {
-        float v = m.data[e];
-        if (v < m.th) {
-            v = 0.f;
-            m.data[e] = 0.f;
-        }
-        if (v != 0.f) {
-            const int k = (int)(e % sz), j = (int)((e / sz) % sy), x = (int)(e / ((size_t)sy * sz));
-            const double a = (double)x - m.c[0], bb = (double)j - m.c[1], c = (double)k - m.c[2];
-            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(bb, bb)), __dmul_rn(c, c));
-            best = d2 > best ? d2 : best;
-            ++cnt;
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        const double w = __shfl_down_sync(0xffffffffu, best, o);
-        best = w > best ? w : best;
-        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    }
-    if ((threadIdx.x & 31) == 0 && cnt > 0) {
-        atomicMax(&m.out[0], (unsigned long long)__double_as_longlong(best));
-        atomicAdd(&m.out[1], cnt);
-    }
+    const int wpb = blockDim.x >> 5;
+    prepare_rows(m.data, m.s[0], m.s[1], m.s[2], m.th, m.c[0], m.c[1], m.c[2], m.out,
+                 (int)(blockIdx.x - m.first) * wpb + (int)(threadIdx.x >> 5), (b.m[i + 1].first - m.first) * wpb);
 }
 
 __global__ void k_init_u64(unsigned long long *p) {
@@ -234,12 +225,12 @@ extern "C" int vesper_prepare_map(float *data, int sx, int sy, int sz, double th
                                   uint64_t *out2, void *stream) {
     if (!data || !cent || !out2 || sx < 1 || sy < 1 || sz < 1)
         return fail(VESPER_ERR_INVALID, "vesper_prepare_map: bad arguments");
+    if ((long long)sx * sy > 0x7fffffffll) return fail(VESPER_ERR_UNSUPPORTED, "vesper_prepare_map: too many rows");
     const double th = threshold < 0 ? 0.0 : threshold;   // th < 0 leaves data unshifted (:73-79)
     cudaStream_t st = (cudaStream_t)stream;
     unsigned long long *acc = (unsigned long long *)out2;
     k_init_u64<<<1, 1, 0, st>>>(acc);
-    const size_t n = (size_t)sx * sy * sz;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    const int blocks = std::max(1, std::min((sx * sy + 31) / 32, 152 * 16));
     k_prepare<<<blocks, 256, 0, st>>>(data, sx, sy, sz, (float)th, cent[0], cent[1], cent[2], acc);
     VG_CHECK_LAUNCH("k_prepare");
     return VESPER_OK;
@@ -252,6 +243,8 @@ extern "C" int vesper_prepare_maps(int nmap, float *const *data, const int *dims
     for (int i = 0; i < nmap; ++i)
         if (!data[i] || dims[3 * i] < 1 || dims[3 * i + 1] < 1 || dims[3 * i + 2] < 1)
             return fail(VESPER_ERR_INVALID, "vesper_prepare_maps: map %d: bad arguments", i);
+        else if ((long long)dims[3 * i] * dims[3 * i + 1] > 0x7fffffffll)
+            return fail(VESPER_ERR_UNSUPPORTED, "vesper_prepare_maps: map %d: too many rows", i);
     if (nmap == 0) return VESPER_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(out, 0, (size_t)nmap * 2 * sizeof(uint64_t), st) != cudaSuccess)
@@ -271,8 +264,8 @@ extern "C" int vesper_prepare_maps(int nmap, float *const *data, const int *dims
             }
             m.th = (float)(thresholds[i] < 0 ? 0.0 : thresholds[i]);   // th < 0 leaves data unshifted (:73-79)
             m.first = blocks;
-            const size_t n = (size_t)m.s[0] * m.s[1] * m.s[2];
-            blocks += (int)std::min<size_t>((n + 2047) / 2048, 1024);   // about 8 voxels per thread
+            const int rows = m.s[0] * m.s[1];
+            blocks += std::max(1, std::min((rows + 31) / 32, 1024));   // 8 warps per block, about 4 rows per warp
         }
         b.m[b.nmap].first = blocks;
         k_prepare_many<<<blocks, 256, 0, st>>>(b);
