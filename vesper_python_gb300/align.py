@@ -221,13 +221,19 @@ class Aligner:
         """vesper_prepare_maps over both maps of every pair: map 2i is pair
         i's first map, 2i + 1 its second; prep [n][4] receives their
         (radius bits, count) pairs in that order."""
-        maps = [(st.src1, p.t, st.cent1) for st in P]
-        maps = [m for st, m1 in zip(P, maps) for m in (m1, (st.src2, p.T, st.cent2))]
-        nm = len(maps)
-        ptrs = (ctypes.c_void_p * nm)(*[m[0].data_ptr() for m in maps])
-        dims = (ctypes.c_int * (3 * nm))(*[int(v) for m in maps for v in m[0].shape])
-        ths = (ctypes.c_double * nm)(*[float(m[1]) for m in maps])
-        cents = (ctypes.c_double * (3 * nm))(*[float(v) for m in maps for v in m[2]])
+        srcs = [t for st in P for t in (st.src1, st.src2)]
+        # the argument arrays depend only on the maps' addresses and shapes and
+        # the thresholds (the centres are half the shapes): kept for a repeat
+        key = (tuple((t.data_ptr(), tuple(t.shape)) for t in srcs), float(p.t), float(p.T))
+        args = self.__dict__.get("_prep_args")
+        if args is None or args[0] != key:
+            maps = [m for st in P for m in ((st.src1, p.t, st.cent1), (st.src2, p.T, st.cent2))]
+            nm = len(maps)
+            args = self._prep_args = (key, nm, (ctypes.c_void_p * nm)(*[m[0].data_ptr() for m in maps]),
+                                      (ctypes.c_int * (3 * nm))(*[int(v) for m in maps for v in m[0].shape]),
+                                      (ctypes.c_double * nm)(*[float(m[1]) for m in maps]),
+                                      (ctypes.c_double * (3 * nm))(*[float(v) for m in maps for v in m[2]]))
+        _, nm, ptrs, dims, ths, cents = args
         _native.check(self.lib.vesper_prepare_maps(nm, ptrs, dims, ths, cents, ctypes.c_void_p(prep.data_ptr()),
                                                    self.dev.stream))
 
@@ -491,9 +497,7 @@ class Aligner:
         return allm, [int(c) for c in counts], dev.to_dev_async(local)
 
     FV_STREAMS = 8
-    LATE_MAX_BATCH = 0       # batch cap of the refinement searches that run on the side streams (0: none)
     GLOBAL_SIDE = True       # the proposal form's global searches on the side streams too
-    GLOBAL_MAX_BATCH = 0     # and their batch cap (0: none)
 
     def _side_streams(self):
         if getattr(self, "_side", None) is None:
@@ -563,8 +567,9 @@ class Aligner:
             S = torch.empty((n, k, nscore), dtype=torch.float32, device=dev.device)
             L = torch.empty((n, k, nscore), dtype=torch.int32, device=dev.device)
             if self.GLOBAL_SIDE and self.group is None and self.profile is None:
-                # the pairs' searches on the side streams (batch capped so that
-                # the concurrent searches' scratch stays near the L2 size)
+                # the pairs' searches on the side streams (capping their batch
+                # at 128, 64 or 32 to keep the concurrent scratch near the L2
+                # size measured slower)
                 cur = torch.cuda.current_stream(dev.device)
                 capturing = torch.cuda.is_current_stream_capturing()
                 side = self._side_streams()
@@ -572,8 +577,7 @@ class Aligner:
                     sd.wait_stream(cur)
                 for i, st in enumerate(P):
                     with torch.cuda.stream(side[i % len(side)]):
-                        self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False,
-                                            max_batch=self.GLOBAL_MAX_BATCH)
+                        self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
                     if not capturing:
                         st.top.record_stream(cur)
                 for sd in side:
@@ -714,7 +718,7 @@ class Aligner:
             d = st.dim
             with torch.cuda.stream(side[i % len(side)]):
                 vg.search_device(st.spec, st.qdata, st.qvec, mode, st.ave, rmats[i], batch=p.batch, dev=dev,
-                                 tuned=True, out=(RS[i], RL[i]), max_batch=self.LATE_MAX_BATCH)
+                                 tuned=True, out=(RS[i], RL[i]))
                 st.rtop = torch.empty(N, dtype=torch.int32, device=dev.device)
                 st.r_rows = torch.empty(N, dtype=torch.int64, device=dev.device)
                 st.r_score = torch.empty(N, dtype=torch.float32, device=dev.device)
@@ -738,7 +742,7 @@ class Aligner:
                     e = torch.cuda.Event(enable_timing=True)
                     e.record()
                     self.pair_events.append(e)
-            st.launches += self._search_launches(d, mode, N * 27, p.batch, self.LATE_MAX_BATCH) + 7
+            st.launches += self._search_launches(d, mode, N * 27, p.batch) + 7
             if not capturing:
                 for tt in (st.rtop, st.r_rows, st.r_score, st.r_lin, st.res):
                     tt.record_stream(cur)    # made on a side stream, read on this one
@@ -929,7 +933,7 @@ class Aligner:
                 # 2 fields + (4 layers + vmajor + top-k) shared by the group + scoring
                 st.launches += 3 + (6 if i == 0 else 0)
 
-    def _global_search(self, p, st, mats, nang, out=None, zscore=True, max_batch=0):
+    def _global_search(self, p, st, mats, nang, out=None, zscore=True):
         """Search of the given rotations, top-N and (subset searches, unless
         the caller batches it) the z-score of the best exact score over the
         subset; all on the device."""
@@ -943,9 +947,8 @@ class Aligner:
             st.scores, st.lin = sc, ln
         else:
             st.scores, st.lin = vg.search_device(st.spec, st.qdata, st.qvec, p.mode, st.ave, mats, batch=p.batch,
-                                                 dev=self.dev, profile=self.profile, tuned=True, out=out,
-                                                 max_batch=max_batch)
-        st.launches += self._search_launches(st.dim, p.mode, int(mats.shape[0]), p.batch, max_batch)
+                                                 dev=self.dev, profile=self.profile, tuned=True, out=out)
+        st.launches += self._search_launches(st.dim, p.mode, int(mats.shape[0]), p.batch)
         st.top = vg.topn_device(st.scores, p.N, dev=self.dev)
         st.launches += 1
         if not zscore:
@@ -956,14 +959,12 @@ class Aligner:
         elif p.proposal is not None:
             st.z = torch.zeros((), dtype=torch.float32, device=self.dev.device)
 
-    def _search_launches(self, dim, mode, nrot, batch, max_batch=0):
+    def _search_launches(self, dim, mode, nrot, batch):
         if batch <= 0:
             from . import autotune
             t = autotune.cached(dim, mode, self.dev)
             if t and t.get("batch"):
                 batch = int(t["batch"])
-                if max_batch > 0:
-                    batch = min(batch, int(max_batch))
         return vg.search_plan(dim, mode, batch, nrot, None, self.dev)[1]
 
     def align_host_many(self, items, p: AlignParams, graph: bool = False):

@@ -442,14 +442,12 @@ _SEARCH_SIZES = {}   # (device, side, mode, mixed, batch, rotations, options) ->
 
 
 def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, batch=0, dev=None, profile=None,
-                  opts=None, tuned=False, out=None, max_batch=0):
+                  opts=None, tuned=False, out=None):
     """vesper_search: (scores f32 [n][nscore], lin int32 [n][nscore]) CUDA tensors,
     written into ``out`` = (scores, lin) when given (contiguous, those shapes).
     With ``profile`` (a dict), vesper_search_profile runs instead and the dict
     receives the per-pass device milliseconds and launch counts.  With
-    ``tuned``, the autotuned launch shape is used, its batch capped at
-    ``max_batch`` when that is positive (searches that run concurrently on
-    several streams keep their scratch within the L2 that way)."""
+    ``tuned``, the autotuned launch shape is used."""
     dev = dev or default_device()
     d = int(data.shape[0])
     code = mode if isinstance(mode, int) else MODE_CODES[mode]
@@ -462,8 +460,6 @@ def search_device(spec, data, vec, mode, ave, rotmats, probs=None, mix=None, bat
             t = autotune.tune(dev, spec, data, vec, mode, ave, rotmats, probs=probs, mix=mix)
             _TUNED[tk] = t
         batch = int(t["batch"])
-        if max_batch > 0 and batch > max_batch:
-            batch = int(max_batch)
         opts = (-1, int(t["cchunk"]), int(t["W"]))
     # per call shape: scores per rotation, the workspace size and the options
     # array (the workspace itself is looked up per call: it belongs to the
