@@ -575,6 +575,88 @@ __global__ void __launch_bounds__(256) k_rpass_c(const PassC2 a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pass C for sides up to 32 with one score group and one score: several
+// x-planes per CTA, whole lines in registers.  Phase y: one (plane, kz) column
+// per thread, its D values read from U, inverse DFT, rows y to shared memory;
+// phase z: one (plane, row pair) per thread, the two rows' half spectra packed
+// into one complex line (Hermitian completion, DC and Nyquist imaginary parts
+// dropped), inverse DFT (real part row 2p, imaginary part row 2p + 1), the
+// scores' first-index argmax keys; one barrier between the phases.  With
+// several planes per CTA both phases keep most threads busy.
+// Used where 4 planes divide the side (measured: side 28 0.078 -> 0.056 us per
+// rotation, side 32 0.096 -> 0.079 against the two-step pass C; at side 30 it
+// took 0.104-0.111 with 2 to 6 planes per CTA against the two-step's 0.093, so
+// side 30 keeps the two-step kernel).  Threads: the y phase's columns rounded
+// up to whole warps.
+template <int D> __host__ __device__ constexpr int line_c_planes() { return 4; }
+template <int D> __host__ __device__ constexpr bool line_c_used() { return D <= 32 && D % line_c_planes<D>() == 0; }
+template <int D> __host__ __device__ constexpr int line_c_threads() {
+    return (line_c_planes<D>() * (D / 2 + 1) + 31) / 32 * 32 > 128 ? 128
+                                                                   : (line_c_planes<D>() * (D / 2 + 1) + 31) / 32 * 32;
+}
+
+template <int D, int PL>
+__host__ __device__ constexpr size_t smem_rc_line() {
+    return (size_t)PL * D * (D / 2 + 1) * sizeof(float2) + 2 * sizeof(unsigned long long);
+}
+
+template <int N1, int N2>
+__global__ void __launch_bounds__(line_c_threads<N1 * N2>()) k_rpass_c_line(const PassC2 a) {
+    constexpr int D = N1 * N2, H = D / 2 + 1, NP = (D + 1) / 2, PL = line_c_planes<D>();
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2 *rows = (float2 *)smem;   // [PL][D][H]
+    unsigned long long *red = (unsigned long long *)(rows + (size_t)PL * D * H);   // [2]
+    const int x0 = blockIdx.x * PL, b = blockIdx.y, r = a.r0 + b;
+    if (threadIdx.x < 2) red[threadIdx.x] = 0ull;
+    // y: inverse DFT of every (plane, kz) column
+    for (int t = threadIdx.x; t < PL * H; t += blockDim.x) {
+        const int pl = t / H, kz = t - pl * H, x = x0 + pl;
+        if (x >= D) continue;
+        const float2 *src = a.U + ((size_t)b * D + x) * (size_t)D * H + kz;
+        float2 v[D];
+#pragma unroll
+        for (int ky = 0; ky < D; ++ky) v[ky] = src[(size_t)ky * H];
+        rdft<D, true>(v);
+        float2 *dst = rows + (size_t)pl * D * H + kz;
+#pragma unroll
+        for (int y = 0; y < D; ++y) dst[(size_t)y * H] = v[y];
+    }
+    __syncthreads();
+    // z: row pairs (2p, 2p + 1), inverse complex DFT, scores
+    unsigned long long best = 0ull;
+    for (int t = threadIdx.x; t < PL * NP; t += blockDim.x) {
+        const int pl = t / NP, p = t - pl * NP, x = x0 + pl, y = 2 * p;
+        if (x >= D) continue;
+        const float2 *r0 = rows + ((size_t)pl * D + y) * H;
+        const bool hb = y + 1 < D;
+        const float2 *r1 = r0 + H;
+        float2 u[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            if (k < H) {
+                float2 A = r0[k], B = hb ? r1[k] : make_float2(0.f, 0.f);
+                if (k == 0 || 2 * k == D) { A.y = 0.f; B.y = 0.f; }
+                u[k] = make_float2(A.x - B.y, A.y + B.x);
+            } else {
+                const float2 A = r0[D - k], B = hb ? r1[D - k] : make_float2(0.f, 0.f);
+                u[k] = make_float2(A.x + B.y, B.x - A.y);
+            }
+        }
+        rdft<D, true>(u);
+        const uint32_t base = (uint32_t)((x * D + y) * D);
+#pragma unroll
+        for (int z = 0; z < D; ++z) {
+            best = max(best, make_key(u[z].x, base + z));
+            if (hb) best = max(best, make_key(u[z].y, base + D + z));
+        }
+    }
+    best = warp_max_u64(best);
+    if ((threadIdx.x & 31) == 0) atomicMax(&red[0], best);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(&a.keys[(size_t)r * a.nscore], red[0]);
+}
+
 // ---- one compiled side of the register passes, as vesper_search.cu calls it ----
 struct RegEntry {
     int mode, d;
@@ -611,7 +693,12 @@ struct RegPath {
         }
     }
     static void c(dim3 g, int T, size_t s, cudaStream_t st, const PassC2 &p, int nscore) {
-        if constexpr (NGRP == 1) {
+        if constexpr (NGRP == 1 && line_c_used<N1 * N2>()) {
+            constexpr int D = N1 * N2, PL = line_c_planes<D>();
+            constexpr size_t sl = smem_rc_line<D, PL>();
+            allow_smem(k_rpass_c_line<N1, N2>, sl);
+            k_rpass_c_line<N1, N2><<<dim3((D + PL - 1) / PL, g.y), line_c_threads<D>(), sl, st>>>(p);
+        } else if constexpr (NGRP == 1) {
             // sides up to 32: a plane's steps have 45 to 160 items, so 64 threads
             // per plane leave fewer idle (measured 0.123 -> 0.096 us per rotation at
             // side 30 against 256 threads; 128 gave 0.101)
