@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(kLineAThreads, 8) k_rpass_a_line(const PassA2 
         float2 v[D];
 #pragma unroll
         for (int j = 0; j < D; ++j) v[j] = line[j];
-        rdft<D, false>(v);
+        rdft<D, false, true>(v);   // largest prime power first (faster here)
         const bool two = 2 * p + 1 < D;
 #pragma unroll
         for (int k = 0; k < H; ++k) {
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(kLineAThreads, 8) k_rpass_a_line(const PassA2 
         float2 v[D];
 #pragma unroll
         for (int y = 0; y < D; ++y) v[y] = pln[(y >> 1) * LS + (y & 1) * Hp];
-        rdft<D, false>(v);
+        rdft<D, false, true>(v);   // largest prime power first (faster here)
         float2 *dst = a.S + (((size_t)b * NCH + c) * D + x) * (size_t)D * H + kz;
 #pragma unroll
         for (int ky = 0; ky < D; ++ky) dst[(size_t)ky * H] = v[ky];
