@@ -556,33 +556,42 @@ class Aligner:
                 st.spec = vg.target_spectra_device(st.tdata, st.tvec, mode, st.ave, dev=dev)
                 st.launches += 2
         if p.proposal is not None:
+            # every pair correlates the subset its pooled side's network scores
+            # select (the same size for all): results in one buffer, the
+            # z-scores of the subsets' best scores in one reduction
             self._mark("proposal")
-            self._proposal_subsets(p, P, mats)
-        self._mark("search")
-        if p.proposal is not None and P and all(st.order is not None for st in P):
-            # equal subsets: results of all pairs in one buffer, the z-scores of
-            # the subsets' best scores in one reduction
-            k = int(P[0].order.shape[0])
+            k = max(1, int(np.ceil(p.proposal_frac * nang)))
             nscore = dev.lib.vesper_search_nscore(vg.MODE_CODES[mode], 0)
             S = torch.empty((n, k, nscore), dtype=torch.float32, device=dev.device)
             L = torch.empty((n, k, nscore), dtype=torch.int32, device=dev.device)
             if self.GLOBAL_SIDE and self.group is None and self.profile is None:
-                # the pairs' searches on the side streams (capping their batch
-                # at 128, 64 or 32 to keep the concurrent scratch near the L2
-                # size measured slower)
+                # each pooled side's pairs are searched on the side streams as
+                # soon as that side's subsets are selected, while the network
+                # scores the next side (capping the searches' batch at 128, 64
+                # or 32 to keep the concurrent scratch near the L2 size measured
+                # slower)
                 cur = torch.cuda.current_stream(dev.device)
                 capturing = torch.cuda.is_current_stream_capturing()
                 side = self._side_streams()
-                for sd in side:
-                    sd.wait_stream(cur)
-                for i, st in enumerate(P):
-                    with torch.cuda.stream(side[i % len(side)]):
-                        self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
-                    if not capturing:
-                        st.top.record_stream(cur)
+                index = {id(st): i for i, st in enumerate(P)}
+
+                def launch(sts):
+                    for st in sts:
+                        i = index[id(st)]
+                        sd = side[i % len(side)]
+                        sd.wait_stream(cur)
+                        with torch.cuda.stream(sd):
+                            self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
+                        if not capturing:
+                            st.top.record_stream(cur)
+
+                self._proposal_subsets(p, P, mats, after_side=launch)
+                self._mark("search")
                 for sd in side:
                     cur.wait_stream(sd)
             else:
+                self._proposal_subsets(p, P, mats)
+                self._mark("search")
                 for i, st in enumerate(P):
                     self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
             sc0 = S[:, :, 0]
@@ -590,8 +599,9 @@ class Aligner:
             for i, st in enumerate(P):
                 st.z = z[i]
         else:
+            self._mark("search")
             for st in P:
-                self._global_search(p, st, mats if st.order is None else st.sub, nang)
+                self._global_search(p, st, mats, nang)
         for st in P:   # the global top-N as grid indices (-1: none)
             if st.order is not None:
                 t = st.top.to(torch.int64)
@@ -908,11 +918,12 @@ class Aligner:
         self.d2h_bytes += packed.numel()
         return [[next(arrays) for _ in g] for g in groups]
 
-    def _proposal_subsets(self, p, P, mats):
+    def _proposal_subsets(self, p, P, mats, after_side=None):
         """Network scores of every rotation and the exact-search subset
         (ascending grid indices) of every pair; all on the device.  Pairs of
         one pooled side share the encoder launches (one per layer for all
-        their maps) and one top-k launch."""
+        their maps) and one top-k launch; ``after_side(pairs)`` is called once
+        a pooled side's subsets are selected."""
         from . import proposal as prop
         dev = self.dev
         pool = int(p.proposal_pool)
@@ -932,6 +943,8 @@ class Aligner:
                 st.sub = subs[i]
                 # 2 fields + (4 layers + vmajor + top-k) shared by the group + scoring
                 st.launches += 3 + (6 if i == 0 else 0)
+            if after_side is not None:
+                after_side(sts)
 
     def _global_search(self, p, st, mats, nang, out=None, zscore=True):
         """Search of the given rotations, top-N and (subset searches, unless
