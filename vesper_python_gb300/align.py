@@ -520,11 +520,25 @@ class Aligner:
         cur = torch.cuda.current_stream(dev.device)
         capturing = torch.cuda.is_current_stream_capturing()   # the graph's pool keeps its blocks
         side = self._side_streams()
+        # with the learned proposal the pairs go to the streams grouped by
+        # pooled side, in the order the network scores the sides, and the
+        # network waits only for its side's pairs (an event per pair), so the
+        # first side is scored while the others' fastVEC still runs
+        overlap = p.proposal is not None and self.GLOBAL_SIDE and self.group is None and self.profile is None
+        order = list(range(n))
+        if overlap:
+            pool = int(p.proposal_pool)
+            first = {}
+            for i, st in enumerate(P):
+                first.setdefault((st.dim + pool - 1) // pool, i)
+            order.sort(key=lambda i: (first[(P[i].dim + pool - 1) // pool], i))
         for sd in side:
             sd.wait_stream(cur)
-        for i, st in enumerate(P):
+        for slot, i in enumerate(order):
+            st = P[i]
             dim = st.dim
-            with torch.cuda.stream(side[i % len(side)]):
+            st.sidx = slot % len(side)
+            with torch.cuda.stream(side[st.sidx]):
                 st.tdata, _, st.tvec = vg.fastvec_device(st.src1, np.float64(np.float32(st.width1)),
                                                          st.o1.astype(np.float64), dim, p.s, st.no1, p.g, dev=dev,
                                                          want_f32=False)
@@ -539,12 +553,16 @@ class Aligner:
                     st.ave = 0.0
                     st.spec = vg.target_spectra_device(st.tdata, st.tvec, mode, st.ave, dev=dev)
                     st.launches += 2
+                if overlap:
+                    st.fv_done = torch.cuda.Event()
+                    st.fv_done.record()
             if not capturing:
                 for t in (st.tdata, st.tvec, st.qdata, st.qvec) + ((st.spec,) if mode not in ("PCC", "CC") else ()):
                     t.record_stream(cur)    # made on a side stream, used on this one
             st.launches += 12
-        for sd in side:
-            cur.wait_stream(sd)
+        if not overlap:
+            for sd in side:
+                cur.wait_stream(sd)
         sh = None
         if mode in ("PCC", "CC"):
             sh = stats.cpu().numpy()
@@ -578,14 +596,14 @@ class Aligner:
                 def launch(sts):
                     for st in sts:
                         i = index[id(st)]
-                        sd = side[i % len(side)]
+                        sd = side[st.sidx]     # the stream of the pair's fastVEC
                         sd.wait_stream(cur)
                         with torch.cuda.stream(sd):
                             self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
                         if not capturing:
                             st.top.record_stream(cur)
 
-                self._proposal_subsets(p, P, mats, after_side=launch)
+                self._proposal_subsets(p, P, mats, after_side=launch, wait=True)
                 self._mark("search")
                 for sd in side:
                     cur.wait_stream(sd)
@@ -918,19 +936,24 @@ class Aligner:
         self.d2h_bytes += packed.numel()
         return [[next(arrays) for _ in g] for g in groups]
 
-    def _proposal_subsets(self, p, P, mats, after_side=None):
+    def _proposal_subsets(self, p, P, mats, after_side=None, wait=False):
         """Network scores of every rotation and the exact-search subset
         (ascending grid indices) of every pair; all on the device.  Pairs of
         one pooled side share the encoder launches (one per layer for all
         their maps) and one top-k launch; ``after_side(pairs)`` is called once
-        a pooled side's subsets are selected."""
+        a pooled side's subsets are selected; with ``wait`` the current
+        stream first waits for each side's pairs' fastVEC (their events)."""
         from . import proposal as prop
         dev = self.dev
         pool = int(p.proposal_pool)
         groups = {}
         for st in P:
             groups.setdefault((st.dim + pool - 1) // pool, []).append(st)
+        cur = torch.cuda.current_stream(dev.device)
         for dp, sts in groups.items():
+            if wait:
+                for st in sts:
+                    cur.wait_event(st.fv_done)
             fTQ = torch.empty((2 * len(sts), 4, dp, dp, dp), dtype=torch.float32, device=dev.device)
             for i, st in enumerate(sts):
                 prop.map_field(st.tdata, st.tvec, pool, dev, out=fTQ[2 * i])
