@@ -511,6 +511,8 @@ class Aligner:
         dev = self.dev
         mode = p.mode
         n = len(P)
+        for st in P:
+            st.tg = None     # made below (each run of the stage, captured or not)
         self._mark("fastvec")
         stats = torch.empty((n, 5), dtype=torch.float64, device=dev.device)
         # fastVEC and statistics of the pairs on FV_STREAMS side streams: one
@@ -600,8 +602,10 @@ class Aligner:
                         sd.wait_stream(cur)
                         with torch.cuda.stream(sd):
                             self._global_search(p, st, st.sub, nang, out=(S[i], L[i]), zscore=False)
+                            st.tg = self._top_grid(st)
                         if not capturing:
                             st.top.record_stream(cur)
+                            st.tg.record_stream(cur)
 
                 self._proposal_subsets(p, P, mats, after_side=launch, wait=True)
                 self._mark("search")
@@ -620,14 +624,18 @@ class Aligner:
             self._mark("search")
             for st in P:
                 self._global_search(p, st, mats, nang)
-        for st in P:   # the global top-N as grid indices (-1: none)
-            if st.order is not None:
-                t = st.top.to(torch.int64)
-                st.tg = torch.where(t >= 0, st.order.to(torch.int64).index_select(0, t.clamp(min=0)),
-                                    torch.full_like(t, -1))
-            else:
-                st.tg = st.top.to(torch.int64)
+        for st in P:   # the global top-N as grid indices (-1: none), where not yet made
+            if st.tg is None:
+                st.tg = self._top_grid(st)
         return stats, sh
+
+    @staticmethod
+    def _top_grid(st):
+        """The pair's global top-N as grid indices (int64, -1: none)."""
+        if st.order is None:
+            return st.top.to(torch.int64)
+        t = st.top.to(torch.int64)
+        return torch.where(t >= 0, st.order.to(torch.int64).index_select(0, t.clamp(min=0)), torch.full_like(t, -1))
 
     _STAGE_FIELDS = ("tdata", "tvec", "qdata", "qvec", "ave", "spec", "order", "sub", "scores", "lin", "top", "z",
                      "tg", "launches")
