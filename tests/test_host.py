@@ -309,3 +309,17 @@ def test_size_grids_matches_size_grid():
     prh[0, 3] = 0
     with pytest.raises(ValueError, match="empty sequence"):
         align._size_grids(prh, cents, widths, origs, s)
+
+
+def test_lattice_angle_inverts_lattice_index():
+    """The aligner's angle of a 5-degree lattice row (the refined models'
+    rotations) is the angle whose lattice row it is, as numpy float64
+    degrees, and repeated rows return the same tuple."""
+    from vesper_python_gb300 import align
+    al = align.Aligner.__new__(align.Aligner)     # no device needed for the lattice arithmetic
+    rng = np.random.default_rng(3)
+    rows = rng.integers(0, vg.LATTICE_N ** 3, size=200).tolist() + [0, vg.LATTICE_N ** 3 - 1]
+    angles = [al._lattice_angle(r) for r in rows]
+    assert all(type(v) is np.float64 for a in angles for v in a)
+    assert vg.lattice_index(np.array(angles)).tolist() == rows
+    assert al._lattice_angle(rows[0]) is angles[0]
