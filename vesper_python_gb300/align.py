@@ -529,11 +529,8 @@ class Aligner:
         overlap = p.proposal is not None and self.GLOBAL_SIDE and self.group is None and self.profile is None
         order = list(range(n))
         if overlap:
-            pool = int(p.proposal_pool)
-            first = {}
-            for i, st in enumerate(P):
-                first.setdefault((st.dim + pool - 1) // pool, i)
-            order.sort(key=lambda i: (first[(P[i].dim + pool - 1) // pool], i))
+            index = {id(st): i for i, st in enumerate(P)}
+            order = [index[id(st)] for _, sts in self._side_groups(P, p) for st in sts]
         for sd in side:
             sd.wait_stream(cur)
         for slot, i in enumerate(order):
@@ -944,6 +941,17 @@ class Aligner:
         self.d2h_bytes += packed.numel()
         return [[next(arrays) for _ in g] for g in groups]
 
+    @staticmethod
+    def _side_groups(P, p):
+        """The pairs grouped by pooled grid side, smallest group first (its
+        searches start soonest), ties in order of first appearance:
+        [(pooled side, [pairs])]."""
+        pool = int(p.proposal_pool)
+        groups = {}
+        for st in P:
+            groups.setdefault((st.dim + pool - 1) // pool, []).append(st)
+        return sorted(groups.items(), key=lambda kv: len(kv[1]))
+
     def _proposal_subsets(self, p, P, mats, after_side=None, wait=False):
         """Network scores of every rotation and the exact-search subset
         (ascending grid indices) of every pair; all on the device.  Pairs of
@@ -954,11 +962,8 @@ class Aligner:
         from . import proposal as prop
         dev = self.dev
         pool = int(p.proposal_pool)
-        groups = {}
-        for st in P:
-            groups.setdefault((st.dim + pool - 1) // pool, []).append(st)
         cur = torch.cuda.current_stream(dev.device)
-        for dp, sts in groups.items():
+        for dp, sts in self._side_groups(P, p):
             if wait:
                 for st in sts:
                     cur.wait_event(st.fv_done)

@@ -699,10 +699,11 @@ struct RegPath {
             allow_smem(k_rpass_c_line<N1, N2>, sl);
             k_rpass_c_line<N1, N2><<<dim3((D + PL - 1) / PL, g.y), line_c_threads<D>(), sl, st>>>(p);
         } else if constexpr (NGRP == 1) {
-            // sides up to 32: a plane's steps have 45 to 160 items, so 64 threads
-            // per plane leave fewer idle (measured 0.123 -> 0.096 us per rotation at
-            // side 30 against 256 threads; 128 gave 0.101)
-            const int t = N1 * N2 <= 32 ? 64 : T;
+            // sides up to 32: a plane's steps have 45 to 160 items, so 96 threads
+            // per plane leave fewer idle (measured at side 30: 0.096 us per rotation
+            // with 64 threads against 0.123 with 256, 0.101 with 128; then 0.089
+            // with 96 against 0.092 with 64 and 0.096 with 32)
+            const int t = N1 * N2 <= 32 ? 96 : T;
             allow_smem(k_rpass_c<1, 1, N1, N2>, s);
             k_rpass_c<1, 1, N1, N2><<<g, t, s, st>>>(p);
         } else if (nscore == 1) {
