@@ -9,7 +9,8 @@ a row: the second call finds the first call's leftovers in the shared
 scratch.  The cases cover the fused kernel (keys only), the register passes
 (the S/U regions), the radix-stage passes in prob mode and the Laplacian
 mode's rotated-density region.  The device's free memory is the same before
-and after a call."""
+and after a call, and a call records into a CUDA graph captured in global
+mode."""
 import ctypes
 
 import numpy as np
@@ -82,6 +83,51 @@ def test_static_search_matches_workspace_search(dev, mode_name, d):
             assert free1 == free0, "device memory changed across the call"
         np.testing.assert_array_equal(sc.cpu().numpy(), ref_sc, err_msg=f"call {call}")
         np.testing.assert_array_equal(ln.cpu().numpy(), ref_ln, err_msg=f"call {call}")
+
+
+@pytest.mark.parametrize("mode_name,d", [("VecProduct", 30), ("prob", 16)])
+def test_static_search_under_global_capture(dev, mode_name, d):
+    """After a first call, vesper_search_static records into a CUDA graph
+    captured in global mode (where an allocation or a synchronizing call would
+    invalidate the capture), and the replayed graph gives the workspace
+    search's results bit for bit."""
+    from vesper_python_gb300 import vesper as vg
+    lib = dev.lib
+    rng = np.random.default_rng(57 + d)
+    tdata, tvec = _field(rng, d)
+    qdata, qvec = _field(rng, d)
+    probs_t = probs_q = None
+    mix = None
+    if mode_name == "prob":
+        probs_t = dev.to_dev(rng.random((4, d, d, d)).astype(np.float32))
+        probs_q = dev.to_dev(np.where(rng.random((4, d, d, d)) < 0.5, rng.random((4, d, d, d)), 0)
+                             .astype(np.float32))
+        mix = (0.5, 2.0, 1.0, 3.0, 4.0)
+    spec = vg.target_spectra_device(dev.to_dev(tdata), dev.to_dev(tvec), mode_name, 0.0, probs=probs_t, dev=dev)
+    mats = dev.to_dev(vg.rot_matrices(orc.calc_angle_comb(30.0)[::7]))
+    qd, qv = dev.to_dev(qdata), dev.to_dev(qvec)
+    ref_sc, ref_ln = vg.search_device(spec, qd, qv, mode_name, 0.0, mats, probs=probs_q, mix=mix, dev=dev)
+    ref_sc = ref_sc.cpu().numpy()
+    ref_ln = ref_ln.cpu().numpy()
+    code = vg.MODE_CODES[mode_name]
+    nscore = lib.vesper_search_nscore(code, 1 if mix is not None else 0)
+    n = int(mats.shape[0])
+    sc = torch.empty((n, nscore), dtype=torch.float32, device=dev.device)
+    ln = torch.empty((n, nscore), dtype=torch.int32, device=dev.device)
+    _static_search(lib, dev, spec, qd, qv, probs_q, d, code, mats, mix, sc, ln)   # per-device and per-side set-up
+    mixarr = (ctypes.c_double * 5)(*mix) if mix is not None else None
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, capture_error_mode="global"):
+        rc = lib.vesper_search_static(_p(spec), _p(qd), _p(qv), _p(probs_q), d, code, 0.0, _p(mats), n, mixarr,
+                                      _p(sc), _p(ln), dev.stream)
+    assert rc == 0, lib.vesper_last_error()
+    for replay in range(2):
+        sc.fill_(float("nan"))
+        ln.fill_(-7)
+        g.replay()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(sc.cpu().numpy(), ref_sc, err_msg=f"replay {replay}")
+        np.testing.assert_array_equal(ln.cpu().numpy(), ref_ln, err_msg=f"replay {replay}")
 
 
 def test_static_search_rejects_oversize(dev):
