@@ -3,7 +3,7 @@
 For a (grid side, mode) pair it times vesper_search_tuned over a sample of
 rotations for every candidate of
 
-  batch      rotations per pipeline step (8 to 128, and up to 2048 while S + U of
+  batch      rotations per pipeline step (8 to 256, and up to 2048 while S + U of
              a step stay within 160 MB)
   cchunk     channels gathered and transformed per pass-A block
   W          spectrum columns per pass-B block
@@ -69,14 +69,19 @@ def _save_disk(entries):
 
 
 BATCHES = (8, 16, 32, 64, 128, 256, 512, 1024, 2048)
-BATCH_BYTES = 160 << 20     # S + U of one batch above 128 rotations: about the L2 size
+# S + U of one batch above 256 rotations: about the L2 size.  Up to 256 every
+# side tries the batch whatever its size: at side 75 (5.1 MB of S per
+# rotation, mode V) 256 rotations ran 8.7 us per rotation against 8.9 with
+# 128 and 11.5 with 16, the largest batch whose S stays in L2, since the S
+# round trip through DRAM costs less than the CTAs a smaller batch leaves idle.
+BATCH_BYTES = 160 << 20
 
 
 def candidates(nch, dim=None, ngrp=1):
     per = None if dim is None else (nch + ngrp) * dim * dim * (dim // 2 + 1) * 8
     out = []
     for batch in BATCHES:
-        if batch > 128 and (per is None or batch * per > BATCH_BYTES):
+        if batch > 256 and (per is None or batch * per > BATCH_BYTES):
             continue
         for cc in sorted({1, nch}):
             for W in (16, 32):
