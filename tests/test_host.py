@@ -323,3 +323,22 @@ def test_lattice_angle_inverts_lattice_index():
     assert all(type(v) is np.float64 for a in angles for v in a)
     assert vg.lattice_index(np.array(angles)).tolist() == rows
     assert al._lattice_angle(rows[0]) is angles[0]
+
+
+def test_autotune_candidates():
+    """Every side tries batches 8..256 with both channel chunks and both
+    column widths; batches above 256 only while one batch's spectra (S + U)
+    stay within the L2-sized cap."""
+    from vesper_python_gb300 import autotune
+    for d, nch, ngrp in ((75, 3, 1), (44, 3, 1), (64, 7, 2), (32, 3, 1), (12, 1, 1)):
+        cands = autotune.candidates(nch, d, ngrp)
+        per = (nch + ngrp) * d * d * (d // 2 + 1) * 8
+        batches = sorted({c["batch"] for c in cands})
+        want = [b for b in autotune.BATCHES if b <= 256 or b * per <= autotune.BATCH_BYTES]
+        assert batches == want
+        assert {8, 16, 32, 64, 128, 256} <= set(batches)
+        for b in batches:
+            shapes = {(c["cchunk"], c["W"]) for c in cands if c["batch"] == b}
+            assert shapes == {(cc, w) for cc in {1, nch} for w in (16, 32)}
+    assert max(c["batch"] for c in autotune.candidates(1, 12, 1)) == 2048
+    assert max(c["batch"] for c in autotune.candidates(3, 75, 1)) == 256
