@@ -286,7 +286,9 @@ int vesper_rescore_batch_dev(const double *tdata, const float *tvec, const doubl
  * vesper_refine_slots: for n pairs with topn global top angles each, given as
  * grid indices tg int64 [n][topn] (-1: none) into grid_rows int64 [ngrid]
  * (each grid angle's row on a lattice of lattice_n steps per axis, row =
- * (x L + y) L + z), and offsets int64 [27][3] in lattice steps: slot
+ * (x L + y) L + z, each in [0, L^3)), and offsets int64 [27][3] in lattice
+ * steps, each in [-L, L) (the kernel reads lattice rows only within these
+ * ranges; the reference's offsets are -1, 0 and +1): slot
  * t = (i topn + k) 27 + o is top k's row plus offset o, valid where
  * x < L, y < L, z < L/2 before negative coordinates wrap by +L and the top
  * exists.  Writes crow int64 [n topn 27] (0 for an invalid slot), valid uint8
