@@ -342,3 +342,46 @@ def test_autotune_candidates():
             assert shapes == {(cc, w) for cc in {1, nch} for w in (16, 32)}
     assert max(c["batch"] for c in autotune.candidates(1, 12, 1)) == 2048
     assert max(c["batch"] for c in autotune.candidates(3, 75, 1)) == 256
+
+
+def test_side_groups_smallest_first_ties_in_order():
+    """Pairs grouped by pooled side, the smallest group first and groups of
+    equal size in order of their first pair."""
+    import types
+    from vesper_python_gb300 import align
+    p = types.SimpleNamespace(proposal_pool=2)
+    P = [types.SimpleNamespace(dim=d, name=i) for i, d in enumerate((28, 30, 32, 30, 28, 30, 27))]
+    groups = align.Aligner._side_groups(P, p)
+    assert [s for s, _ in groups] == [16, 14, 15]
+    assert [[st.name for st in g] for _, g in groups] == [[2], [0, 4, 6], [1, 3, 5]]
+    P2 = [types.SimpleNamespace(dim=d) for d in (32, 28)]
+    assert [s for s, _ in align.Aligner._side_groups(P2, p)] == [16, 14]
+
+
+def test_batch_sig_tracks_what_a_captured_stage_reads():
+    """The graph cache key changes with any map address or shape, grid
+    geometry, parameter or angle grid, and not otherwise."""
+    import dataclasses
+    import types
+
+    import torch
+
+    from vesper_python_gb300 import align
+
+    def pair(a, b, dim=30, w=1.0):
+        return types.SimpleNamespace(src1=a, src2=b, dim=dim, no1=np.array([1.0, 2.0, 3.0]),
+                                     no2=np.array([4.0, 5.0, 6.0]), width1=w, width2=w,
+                                     o1=np.array([0.0, 0.0, 0.0]), o2=np.array([1.0, 1.0, 1.0]))
+    m1, m2, m3 = torch.zeros(8, 8, 8), torch.zeros(4, 4, 4), torch.zeros(4, 4, 4)
+    mats, mats2 = torch.zeros(10, 3, 3), torch.zeros(10, 3, 3)
+    p = align.AlignParams()
+    sig = align.Aligner._batch_sig
+    base = sig([pair(m1, m2)], p, mats)
+    assert sig([pair(m1, m2)], p, mats) == base
+    assert sig([pair(m1, m3)], p, mats) != base                    # another query map buffer
+    assert sig([pair(m1, m2, dim=32)], p, mats) != base            # another grid side
+    assert sig([pair(m1, m2, w=2.0)], p, mats) != base             # another voxel width
+    assert sig([pair(m1, m2), pair(m1, m2)], p, mats) != base      # another pair count
+    assert sig([pair(m1, m2)], p, mats2) != base                   # another angle grid
+    assert sig([pair(m1, m2)], dataclasses.replace(p, N=p.N + 1), mats) != base
+    assert sig([pair(m1, m2)], dataclasses.replace(p, A=p.A + 5), mats) != base
