@@ -229,7 +229,8 @@ int vesper_search_plan(int dim, int mode, int batch, int nrot, const int *opts, 
  * first call on each device looks up the array's device address, and the
  * first call for each (mode, dim) loads that side's kernels and sets their
  * shared-memory limits: make one call for every (mode, dim) you will use
- * before any stream capture.  All calls share the array, so calls that
+ * before any stream capture; after it, a call may itself be recorded into a
+ * CUDA graph captured in global mode.  All calls share the array, so calls that
  * overlap on the GPU (other streams or host threads) race: serialise them. */
 int vesper_search_static(const void *spectra, const double *data, const float *vec, const float *probs, int dim,
                          int mode, double ave, const float *rotmats, int nrot, const double *mix, float *scores_out,
