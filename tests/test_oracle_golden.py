@@ -1,5 +1,6 @@
 """The CPU oracle against the golden vectors recorded from the unmodified
-reference (tests/golden/make_golden.py).  No GPU needed."""
+reference (tests/golden/make_golden.py, make_golden_configs.py and
+make_golden_interp.py).  No GPU needed."""
 import hashlib
 import os
 
@@ -296,3 +297,94 @@ def test_fastvec_noncubic_sources(golden_dir):
         assert np.array_equal(data != 0, rd != 0)
         assert np.max(np.abs(data - rd) / np.maximum(np.abs(rd), 1e-300)) < 1e-15
         assert np.array_equal(vec, g[f"c{i}_vec"])
+
+
+# ---------------------------------------------------------------------------
+# The benchmarked configurations (make_golden_configs.py: the unmodified
+# reference over the full angle grids).  The oracle is checked bit for bit on
+# rotations spread over each grid and over each refinement set; the GPU tests
+# compare every rotation.
+# ---------------------------------------------------------------------------
+def _dense(g, prefix):
+    """A fixture field stored sparse (flat indices of its non-zero voxels
+    and their values) as a dense array."""
+    shape = tuple(int(v) for v in g[f"{prefix}_shape"])
+    val = g[f"{prefix}_val"]
+    out = np.zeros((int(np.prod(shape[:3])),) + shape[3:], val.dtype)
+    out[g[f"{prefix}_idx"]] = val
+    return out.reshape(shape)
+
+
+def _spread(n, k):
+    return np.unique(np.linspace(0, n - 1, k).astype(int))
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_pair200_sampled_rotations_bit_exact(golden_dir, mode):
+    """The 200^3 / 100^3 pair at s = 2 (grid side 75), A = 10."""
+    g = _g(golden_dir, "search_pair200.npz")
+    s1 = g["stats1"]
+    assert int(g["dim"]) == 75
+    ts = orc.target_spectra(orc.mode_field(mode, _dense(g, "data1"), _dense(g, "vec1"), s1[2]))
+    qd, qv = _dense(g, "data2"), _dense(g, "vec2")
+    scale = orc.score_scale(mode, s1[3], s1[4])
+    grid = orc.calc_angle_comb(10.0)
+    assert len(grid) == len(g[f"{mode}_score"]) == 24624
+    for angles, key in ((grid, ""), (g[f"{mode}_refine_angles"], "refine_")):
+        sel = _spread(len(angles), 16)
+        sc, tr = orc.search(ts, mode, qd, qv, angles[sel], s1[2])
+        assert np.array_equal(sc.astype(np.float64) * scale, g[f"{mode}_{key}score"][sel]), key or "global"
+        assert np.array_equal(tr, g[f"{mode}_{key}trans"][sel]), key or "global"
+    # the refinement set is that of the reference's own global top-10, and
+    # the refined models its top-10
+    top = orc.topn(np.asarray(g[f"{mode}_score"], np.float64), 10)
+    assert np.array_equal(orc.refine_angles(grid[top]), g[f"{mode}_refine_angles"])
+    rtop = orc.topn(np.asarray(g[f"{mode}_refine_score"], np.float64), 10)
+    assert np.array_equal(g[f"{mode}_refine_angles"][rtop], g[f"{mode}_refined_angle"])
+
+
+def test_prob_pad64_sampled_rotations_bit_exact(golden_dir):
+    """The prob pair with every grid padded to 64^3, A = 15: both passes and
+    the refinement set."""
+    g = _g(golden_dir, "prob_pair128_pad64.npz")
+    d = int(g["dim"])
+    assert d == 64
+    tvec, tprobs = _dense(g, "vec1"), np.moveaxis(_dense(g, "probs1"), 3, 0).copy()
+    qd, qv, qp = _dense(g, "data2"), _dense(g, "vec2"), list(np.moveaxis(_dense(g, "probs2"), 3, 0).copy())
+    tspec = orc.target_spectra([tvec[..., 0], tvec[..., 1], tvec[..., 2]] + list(tprobs))
+    grid = orc.calc_angle_comb(15.0)
+    assert len(grid) == len(g["pass1_vscore"])
+    for r in _spread(len(grid), 12):
+        vs, vt, ps, pt, _, _ = orc.rot_and_search_prob(tspec, qd, qv, qp, grid[r], 0.5)
+        assert np.float64(vs) == g["pass1_vscore"][r] and tuple(vt) == tuple(g["pass1_vtrans"][r])
+        assert np.float64(ps) == g["pass1_pscore"][r] and tuple(pt) == tuple(g["pass1_ptrans"][r])
+    st = orc.prob_stats(g["pass1_vscore"], g["pass1_pscore"], 1.0 / d ** 3)
+    for r in _spread(len(grid), 12):
+        res = orc.rot_and_search_prob(tspec, qd, qv, qp, grid[r], 0.5, st)
+        assert np.float64(res[4]) == g["pass2_mscore"][r] and tuple(res[5]) == tuple(g["pass2_mtrans"][r])
+    ra = g["refine_angles"]
+    assert np.array_equal(ra, orc.refine_angles(grid[orc.topn(g["pass2_mscore"], 10)]))
+    for r in _spread(len(ra), 8):
+        res = orc.rot_and_search_prob(tspec, qd, qv, qp, ra[r], 0.5, st)
+        assert np.float64(res[4]) == g["refine_mscore"][r] and tuple(res[5]) == tuple(g["refine_mtrans"][r])
+
+
+def test_uneven_sides_sampled_rotations_bit_exact(golden_dir):
+    """One pair of the uneven 64-pair batch for every grid side it produces
+    (11 ... 44, fused sides included), s = 4, A = 15, mode V."""
+    g = _g(golden_dir, "uneven_sides.npz")
+    grid = orc.calc_angle_comb(15.0)
+    sides = [int(s) for s in g["sides"]]
+    assert {11, 18, 22, 44} <= set(sides)
+    for side in sides:
+        pre = f"d{side}_"
+        assert int(g[pre + "dim"]) == side
+        s1 = g[pre + "stats1"]
+        ts = orc.target_spectra(orc.mode_field("V", _dense(g, pre + "data1"), _dense(g, pre + "vec1"), s1[2]))
+        qd, qv = _dense(g, pre + "data2"), _dense(g, pre + "vec2")
+        scale = orc.score_scale("V", s1[3], s1[4])
+        for angles, key in ((grid, ""), (g[pre + "refine_angles"], "refine_")):
+            sel = _spread(len(angles), 8)
+            sc, tr = orc.search(ts, "V", qd, qv, angles[sel], s1[2])
+            assert np.array_equal(sc.astype(np.float64) * scale, g[pre + key + "score"][sel]), (side, key)
+            assert np.array_equal(tr, g[pre + key + "trans"][sel]), (side, key)
