@@ -388,3 +388,31 @@ def test_uneven_sides_sampled_rotations_bit_exact(golden_dir):
             sc, tr = orc.search(ts, "V", qd, qv, angles[sel], s1[2])
             assert np.array_equal(sc.astype(np.float64) * scale, g[pre + key + "score"][sel]), (side, key)
             assert np.array_equal(tr, g[pre + key + "trans"][sel]), (side, key)
+
+
+@pytest.mark.parametrize("mode", ["V", "O", "C", "P", "L"])
+def test_pair200_refined_models_match_reference_prints(golden_dir, mode):
+    """At side 75 (the 200^3 / 100^3 pair, s = 2): the oracle's get_score
+    and convert_trans over the reference's refined models reproduce its
+    printed get_score lines and model translations."""
+    import re
+    g = _g(golden_dir, "search_pair200.npz")
+    txt = open(f"{golden_dir}/search_pair200_{mode}.txt").read()
+    printed = re.findall(r"Overlap=(\S+) (\d+)/(\d+) CC=(\S+) PCC=(\S+)\nScore= (\S+)", txt)
+    rows = re.findall(r"\n#(\d+) Rotation= \((\S+) (\S+) (\S+)\) Translation= \((\S+) (\S+) (\S+)\)", txt)
+    angles, trans = g[f"{mode}_refined_angle"], g[f"{mode}_refined_trans"]
+    assert len(printed) == len(rows) == len(angles) > 0
+    d1, v1, d2, v2 = _dense(g, "data1"), _dense(g, "vec1"), _dense(g, "data2"), _dense(g, "vec2")
+    st1 = g["stats1"]
+    d = int(g["dim"])
+    for k in range(len(angles)):
+        vec, data = orc.rot_mrc(d2, v2, angles[k])
+        ov, nm, total, cc, pcc, score, _ = orc.get_score(d1, v1, st1[2], st1[3], st1[4], data, vec, trans[k])
+        p_ov, p_nm, p_total, p_cc, p_pcc, p_score = printed[k]
+        assert (nm, total) == (int(p_nm), int(p_total))
+        assert ov == float(p_ov)
+        for got, want in ((cc, p_cc), (pcc, p_pcc), (score, p_score)):
+            assert abs(got - float(want)) <= 1e-12 * max(1.0, abs(float(want))), (k, got, want)
+        assert int(rows[k][0]) == k and np.allclose([float(v) for v in rows[k][1:4]], angles[k])
+        t = orc.convert_trans(g["cent1"], g["cent2"], orc.euler2rot(angles[k]), trans[k], 2.0, d)
+        assert ["{:.3f}".format(v) for v in t] == list(rows[k][4:7]), (k, t, rows[k])
