@@ -416,3 +416,31 @@ def test_pair200_refined_models_match_reference_prints(golden_dir, mode):
         assert int(rows[k][0]) == k and np.allclose([float(v) for v in rows[k][1:4]], angles[k])
         t = orc.convert_trans(g["cent1"], g["cent2"], orc.euler2rot(angles[k]), trans[k], 2.0, d)
         assert ["{:.3f}".format(v) for v in t] == list(rows[k][4:7]), (k, t, rows[k])
+
+
+def test_uneven_sides_refined_models_match_reference_prints(golden_dir):
+    """Every grid side of the uneven batch (s = 4, mode V): the oracle's
+    get_score and convert_trans over the reference's refined models
+    reproduce its printed lines."""
+    import re
+    g = _g(golden_dir, "uneven_sides.npz")
+    for side in [int(s) for s in g["sides"]]:
+        pre = f"d{side}_"
+        txt = str(g[pre + "stdout"])
+        printed = re.findall(r"Overlap=(\S+) (\d+)/(\d+) CC=(\S+) PCC=(\S+)\nScore= (\S+)", txt)
+        rows = re.findall(r"\n#(\d+) Rotation= \((\S+) (\S+) (\S+)\) Translation= \((\S+) (\S+) (\S+)\)", txt)
+        angles, trans = g[pre + "refined_angle"], g[pre + "refined_trans"]
+        assert len(printed) == len(rows) == len(angles) > 0, side
+        d1, v1 = _dense(g, pre + "data1"), _dense(g, pre + "vec1")
+        d2, v2 = _dense(g, pre + "data2"), _dense(g, pre + "vec2")
+        st1 = g[pre + "stats1"]
+        for k in range(len(angles)):
+            vec, data = orc.rot_mrc(d2, v2, angles[k])
+            ov, nm, total, cc, pcc, score, _ = orc.get_score(d1, v1, st1[2], st1[3], st1[4], data, vec, trans[k])
+            p_ov, p_nm, p_total, p_cc, p_pcc, p_score = printed[k]
+            assert (nm, total) == (int(p_nm), int(p_total)), (side, k)
+            assert ov == float(p_ov), (side, k)
+            for got, want in ((cc, p_cc), (pcc, p_pcc), (score, p_score)):
+                assert abs(got - float(want)) <= 1e-12 * max(1.0, abs(float(want))), (side, k, got, want)
+            t = orc.convert_trans(g[pre + "cent1"], g[pre + "cent2"], orc.euler2rot(angles[k]), trans[k], 4.0, side)
+            assert ["{:.3f}".format(v) for v in t] == list(rows[k][4:7]), (side, k, t, rows[k])
