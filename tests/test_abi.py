@@ -85,3 +85,63 @@ def test_topk_subset_batch_rejects_bad_args():
     assert lib.vesper_topk_subset_batch(None, 2, 100, 5, None, None) == 1
     assert lib.vesper_topk_subset_batch(1, 0, 100, 5, 1, None) == 1
     assert lib.vesper_topk_subset_batch(1, 2, 100, 101, 1, None) == 1
+
+
+def _header_params():
+    """{name: [parameter kind]} from the header: p pointer, z size_t,
+    d double, l 64-bit integer, i int."""
+    txt = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\b(?:int|const char \*)\s*\*?\s*(vesper_\w+)\s*\(([^)]*)\)\s*;", txt):
+        kinds = []
+        for prm in [p.strip() for p in params.split(",") if p.strip() and p.strip() != "void"]:
+            if "*" in prm:
+                kinds.append("p")
+            elif prm.startswith("size_t"):
+                kinds.append("z")
+            elif prm.startswith("double"):
+                kinds.append("d")
+            elif re.match(r"(u?int64_t|long long)\b", prm):
+                kinds.append("l")
+            else:
+                kinds.append("i")
+        out[name] = kinds
+    return out
+
+
+def _ctypes_kind(t):
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(t, ctypes._Pointer)):
+        return "p"
+    if t is ctypes.c_size_t:
+        return "z"
+    if t is ctypes.c_double:
+        return "d"
+    if t in (ctypes.c_int64, ctypes.c_longlong, ctypes.c_uint64) and ctypes.sizeof(t) == 8 and t is not ctypes.c_int:
+        return "l"
+    return "i"
+
+
+def test_python_binding_matches_header_parameters():
+    """Every ctypes signature the package binds has the header's parameter
+    count and kinds (pointer, size_t, double, 64-bit or plain int)."""
+    hdr = _header_params()
+    assert set(hdr) == set(declared_symbols())
+    for name, kinds in hdr.items():
+        got = [_ctypes_kind(t) for t in _native.SIGNATURES[name]]
+        assert got == kinds, (name, got, kinds)
+
+
+def test_integration_stub_matches_header_parameters():
+    """The ctypes stub a maintainer of the reference would add (the binding
+    shown in INTEGRATION.md) declares each function with the header's
+    parameter count and kinds."""
+    path = os.path.join(os.path.dirname(_native.INCLUDE), "INTEGRATION.md")
+    if not os.path.exists(path):
+        pytest.skip("integration guide not present")
+    hdr = _header_params()
+    lines = re.findall(r"lib\.(vesper_\w+)\.argtypes = \[(.*)\]", open(path).read())
+    assert lines
+    names = {"vp": "p", "i32": "i", "f64": "d", "sz": "z", "ctypes.POINTER(sz)": "p"}
+    for name, args in lines:
+        got = [names[a.strip()] for a in args.split(",") if a.strip()]
+        assert got == hdr[name], (name, got, hdr[name])
